@@ -1,0 +1,226 @@
+/*
+ * mcrt.h - C ABI of libmcrt, a GB300 (sm_103a) engine for polarised Monte Carlo
+ * radiative transfer with coherent backscattering (CB).
+ *
+ * It is a drop-in for the GPU branch of the reference package's driver
+ * `simulate(cfg, g, I0; use_gpu)` (MonteCarloRadiativeTransfer.jl,
+ * src/MonteCarloRadiativeTransfer.jl:26-85): the package keeps its Config, scatterer and
+ * geometry types and its run_rt entry point, and ccalls this library where the
+ * reference launches its CUDA.jl kernel (src/MonteCarloRadiativeTransfer.jl:36-56).
+ *
+ * Conventions
+ *   - Every call returns an int status (MCRT_OK = 0); mcrt_last_error() gives a
+ *     message for the calling thread's last failure.
+ *   - All arrays are plain host pointers owned by the caller; the library copies what
+ *     it keeps. Tally outputs use the reference's Julia column-major layouts:
+ *     Irt[4, Ntheta, Nphi] and Icb[4, Ntheta_b, Nphi_b], i.e. element (s, j1, j2) at
+ *     s + 4*(j1 + Ntheta*j2), zero-based here.
+ *   - Invalid geometry or configuration returns MCRT_EINVAL with the reference's
+ *     validate() messages (src/geometries/plane.jl:52-62, sphere.jl:35-37), where a
+ *     Julia caller rethrows ArgumentError.
+ *   - There is no CPU fallback: without a usable CUDA device the compute calls return
+ *     MCRT_ENODEV.
+ */
+#ifndef MCRT_H
+#define MCRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCRT_ABI_VERSION 1
+
+enum mcrt_status_code {
+  MCRT_OK = 0,
+  MCRT_EINVAL = 1,    /* bad argument; message via mcrt_last_error() */
+  MCRT_ENOMEM = 2,    /* device or host allocation failed */
+  MCRT_ECUDA = 3,     /* CUDA runtime error */
+  MCRT_ENONCONV = 4,  /* a capped device loop gave up (see mcrt_stats.status_flags) */
+  MCRT_ETIMEDOUT = 5, /* a wait ran out of time */
+  MCRT_EBUSY = 6,     /* admission refused: over the memory cap or out of slots */
+  MCRT_ENOTFOUND = 7, /* unknown ticket */
+  MCRT_ENODEV = 8     /* no CUDA device */
+};
+
+enum mcrt_scatterer_kind { MCRT_RAYLEIGH = 0, MCRT_MIE = 1 };
+enum mcrt_geometry_kind { MCRT_PLANE = 0, MCRT_SPHERE = 1 };
+enum mcrt_precision { MCRT_FP32 = 0, MCRT_FP64 = 1 };
+enum mcrt_kernel_kind {
+  MCRT_KERNEL_PERSISTENT = 0, /* event-batched persistent kernel (the fast path) */
+  MCRT_KERNEL_PLAIN = 1       /* one thread per ray, the structure of src/gpu.jl:177-296 */
+};
+enum mcrt_rng_mode {
+  MCRT_RNG_PHILOX = 0,           /* Philox4x32-10 keyed by (seed, instance) */
+  MCRT_RNG_STRATIFIED_DEPTH = 1  /* test mode: first-collision depth draw = (i+0.5)/N */
+};
+/* Bits of mcrt_stats.status_flags */
+enum mcrt_status_flags {
+  MCRT_FLAG_REJECT_LIMIT = 1, /* a rejection loop (src/gpu.jl:215-256) hit its cap */
+  MCRT_FLAG_KEPLER_CAP = 2,   /* kepler_solver (src/utils.jl:243-261) hit its cap */
+  MCRT_FLAG_NONFINITE = 4     /* a non-finite photon weight was dropped */
+};
+
+typedef struct mcrt_ctx mcrt_ctx;
+typedef struct mcrt_scatterer mcrt_scatterer;
+typedef struct mcrt_solve mcrt_solve;
+typedef struct mcrt_batch mcrt_batch;
+typedef struct mcrt_server mcrt_server;
+
+/* Scatterer: RayleighScatterer (src/scatterers/rayleigh.jl:3-6) or the tables of
+ * MieScatterer (src/scatterers/mie.jl:3-15). Mie tables are stored on the device in
+ * FP32 (both precisions read the same stored values). */
+typedef struct {
+  int kind;        /* mcrt_scatterer_kind */
+  double omega;    /* single-scattering albedo */
+  double kl;       /* mean free path (the CB phase scale, src/gpu.jl:102) */
+  int n_theta;     /* Mie: table length on the uniform grid 0..pi */
+  const double *F11, *F12, *F33, *F34; /* Mie: n_theta each */
+  const double *S11, *S22;             /* Mie: 2*n_theta each, interleaved (re, im) */
+  int random_points;                   /* Mie: csrn has random_points + 1 entries */
+  const double* csrn;                  /* Mie: inverse CDF of cos(theta) */
+} mcrt_scatterer_desc;
+
+/* Config (src/config.jl:55-124); the trigonometric and weight arrays are passed in. */
+typedef struct {
+  int64_t number_of_rays;
+  double minimum_intensity;
+  int64_t maximum_scattering_times;
+  int64_t maximum_threads; /* used by the plain kernel only, as in the reference */
+  int compute_cb;
+  double tau0;
+  int n_phi;
+  const double *cos_phi, *sin_phi;
+  int n_theta;
+  const double *cos_theta, *sin_theta, *inorm;
+  int n_theta_b;
+  const double *cos_theta_b, *sin_theta_b;
+  int n_phi_b;
+  const double *cos_phi_b, *sin_phi_b;
+} mcrt_config;
+
+/* Layer (src/geometries/plane.jl:6-21); for a sphere the single layer's tau is the
+ * optical radius (src/geometries/sphere.jl:6-21). */
+typedef struct {
+  double tau;
+  double omega;
+  int infinite; /* plane only: a semi-infinite last layer (d < 0) */
+  const mcrt_scatterer* scatterer;
+} mcrt_layer;
+
+typedef struct {
+  int kind;            /* mcrt_geometry_kind */
+  double theta, phi;   /* plane incidence angles; ignored for a sphere (pi, 0) */
+  int n_layers;        /* sphere: 1 */
+  const mcrt_layer* layers;
+} mcrt_geometry;
+
+/* Launch options; zero-initialised means: FP32, persistent kernel, Philox, autotuned. */
+typedef struct {
+  int precision;        /* mcrt_precision */
+  int kernel;           /* mcrt_kernel_kind */
+  uint64_t seed;
+  uint32_t instance;    /* Philox key word (one per simulate call of a run_rt) */
+  int rng_mode;         /* mcrt_rng_mode */
+  int64_t photon_begin; /* first photon index (sub-runs continue a stream) */
+  int block_size;       /* persistent: 0 = autotuned; 128, 256 or 512 */
+  int blocks_per_sm;    /* persistent: 0 = autotuned */
+  int plain_threads;    /* plain: 0 = min(maximum_threads, number_of_rays) */
+} mcrt_run_opts;
+
+/* Diagnostics returned beside the tallies (all raw sums over the photons run). */
+typedef struct {
+  double cb_peak_sum;    /* per-photon sum of its CB peak (s11 at theta_b = 0) */
+  double cb_peak_sumsq;  /* per-photon sum of squares of the same */
+  double photons;
+  double events;         /* scattering events */
+  double attempts;       /* rejection-loop attempts */
+  double rt_evals;       /* RT peel-off bin evaluations */
+  double cb1_evals;      /* CB single-scattering bin evaluations */
+  double cbn_evals;      /* CB reciprocal-path bin evaluations */
+  double kernel_ms;      /* device time of the transport launch (CUDA events) */
+  int status_flags;      /* mcrt_status_flags */
+  int block_size, blocks; /* launch shape that ran */
+} mcrt_stats;
+
+/* ------------------------------------------------------------------ basics */
+int mcrt_abi_version(void);
+const char* mcrt_last_error(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int mcrt_device_count(void);
+
+/* Context bound to one device: streams, autotuner cache, scratch pools. */
+int mcrt_ctx_create(int device, mcrt_ctx** out);
+int mcrt_ctx_destroy(mcrt_ctx* ctx);
+
+/* Uploads the scatterer (replaces the adapt(CuArray, ...) of
+ * src/MonteCarloRadiativeTransfer.jl:92-99,194-199). */
+int mcrt_scatterer_create(mcrt_ctx* ctx, const mcrt_scatterer_desc* desc, mcrt_scatterer** out);
+int mcrt_scatterer_destroy(mcrt_scatterer* s);
+
+/* Host-side table producer for MieScatterer(r, m, lambda, nu; Ntheta, random_points)
+ * (src/scatterers/mie.jl:36-44, bhmie :129-216, calculate_csrn src/utils.jl:263-287).
+ * Outputs: omega, kl; F11,F12,F33,F34 (n_theta each); S11,S22 (2*n_theta, re/im);
+ * csrn (random_points+1); q[5] = (q_ext, q_sca, q_abs, q_back, asymm). No GPU needed. */
+int mcrt_mie_tables(double r, double m_re, double m_im, double lambda, double nu, int n_theta,
+                    int random_points, double* omega, double* kl, double* F11, double* F12,
+                    double* F33, double* F34, double* S11, double* S22, double* csrn, double* q);
+
+/* ------------------------------------------------------------------ simulate */
+/* The drop-in for simulate(cfg, g, I0; use_gpu=true): runs cfg.number_of_rays photons
+ * and returns A_out = (Adt, Aabs, Aref, Atrans, Arem), Irt and Icb, all divided by
+ * number_of_rays as src/MonteCarloRadiativeTransfer.jl:78-84 does. Icb_ladder
+ * (optional, Ntheta_b*Nphi_b) is the incoherent s11 counterpart of Icb; stats is
+ * optional. Synchronous, like the reference (which syncs at :51-56). */
+int mcrt_simulate(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g,
+                  const double I0[4], const mcrt_run_opts* opts, double A_out[5], double* Irt,
+                  double* Icb, double* Icb_ladder, mcrt_stats* stats);
+
+/* ------------------------------------------------------------------ resident solves */
+/* A solve keeps its inputs (bin tables, instance descriptor) and its FP64 tallies
+ * resident in device memory, so it can be run repeatedly without host traffic. */
+int mcrt_solve_create(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g,
+                      const double I0[4], const mcrt_run_opts* opts, mcrt_solve** out);
+/* Zeroes the tallies and launches the transport of n_photons photons starting at
+ * photon index photon_begin, asynchronously on the context's stream. */
+int mcrt_solve_launch(mcrt_solve* s, int64_t photon_begin, int64_t n_photons);
+/* Waits for the solve and copies raw (undivided) sums to the host; any pointer may be
+ * NULL. */
+int mcrt_solve_read(mcrt_solve* s, double A_out[5], double* Irt, double* Icb, double* Icb_ladder,
+                    mcrt_stats* stats);
+int mcrt_solve_destroy(mcrt_solve* s);
+
+/* ------------------------------------------------------------------ batched launch */
+/* Many independent simulate() instances (each with its own geometry, scatterers,
+ * incident Stokes vector, seed and photon budget) run in one persistent launch from
+ * per-instance work queues. Instances of one batch share the config's bin grids. */
+typedef struct {
+  const mcrt_geometry* geometry;
+  double I0[4];
+  uint64_t seed;
+  uint32_t instance;
+  int64_t n_photons;
+} mcrt_instance;
+
+int mcrt_batch_create(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_instance* inst,
+                      int n_inst, const mcrt_run_opts* opts, mcrt_batch** out);
+int mcrt_batch_launch(mcrt_batch* b);
+/* Per-instance raw sums for instance i (any output pointer may be NULL). */
+int mcrt_batch_read(mcrt_batch* b, int i, double A_out[5], double* Irt, double* Icb,
+                    double* Icb_ladder, mcrt_stats* stats);
+/* Device time of the last launch and the total photons it ran. */
+int mcrt_batch_timing(mcrt_batch* b, double* kernel_ms, double* photons);
+int mcrt_batch_destroy(mcrt_batch* b);
+
+/* ------------------------------------------------------------------ measurement */
+/* Measured FP32 FMA throughput of this device (TFLOP/s, FMA = 2 flops) from a short
+ * dependent-FMA microbenchmark; used as the roofline peak of the transport kernel. */
+int mcrt_measure_fp32_peak(mcrt_ctx* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCRT_H */

@@ -1,0 +1,931 @@
+// C ABI of libmcrt (declared in include/mcrt.h): device context, scatterer upload,
+// resident solves, batched persistent launches and the drop-in mcrt_simulate.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mcrt.h"
+#include "mcrt_device.cuh"
+#include "mcrt_host.h"
+#include "mcrt_kernels.h"
+
+using namespace mcrt;
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return set_err(e_ == cudaErrorMemoryAllocation ? MCRT_ENOMEM : MCRT_ECUDA,          \
+                     std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t bytes) {
+    release();
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) n = bytes;
+    else p = nullptr;
+    return e;
+  }
+  template <typename U>
+  U* as() const {
+    return reinterpret_cast<U*>(p);
+  }
+};
+
+}  // namespace
+
+// ================================================================== context / scatterers
+struct mcrt_ctx {
+  int device = 0;
+  int sms = 0;
+  int smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::mutex mu;
+  std::map<std::string, std::pair<int, int>> tuned;  // signature -> (block size, blocks/SM)
+};
+
+struct mcrt_scatterer {
+  mcrt_ctx* ctx = nullptr;
+  int kind = 0;
+  double omega = 1, kl = 1;
+  int ntheta = 0, rp = 0;
+  DevBuf F, S, C;
+  DevScatterer view() const {
+    DevScatterer d{};
+    d.kind = kind;
+    d.ntheta = ntheta;
+    d.rp = rp;
+    d.kl = kl;
+    d.F = F.as<const float4>();
+    d.S = S.as<const float4>();
+    d.csrn = C.as<const float>();
+    return d;
+  }
+};
+
+extern "C" {
+
+int mcrt_abi_version(void) { return MCRT_ABI_VERSION; }
+
+const char* mcrt_last_error(void) { return g_err.c_str(); }
+
+int mcrt_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int mcrt_ctx_create(int device, mcrt_ctx** out) {
+  if (!out) return set_err(MCRT_EINVAL, "mcrt_ctx_create: out is NULL");
+  *out = nullptr;
+  int n = mcrt_device_count();
+  if (n <= 0) return set_err(MCRT_ENODEV, "no CUDA device is visible");
+  if (device < 0 || device >= n) return set_err(MCRT_EINVAL, "device index out of range");
+  std::unique_ptr<mcrt_ctx> c(new mcrt_ctx());
+  c->device = device;
+  CK(cudaSetDevice(device));
+  CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device));
+  CK(cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&c->e0));
+  CK(cudaEventCreate(&c->e1));
+  *out = c.release();
+  return MCRT_OK;
+}
+
+int mcrt_ctx_destroy(mcrt_ctx* ctx) {
+  if (!ctx) return MCRT_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->e0) cudaEventDestroy(ctx->e0);
+  if (ctx->e1) cudaEventDestroy(ctx->e1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MCRT_OK;
+}
+
+int mcrt_scatterer_create(mcrt_ctx* ctx, const mcrt_scatterer_desc* d, mcrt_scatterer** out) {
+  if (!ctx || !d || !out) return set_err(MCRT_EINVAL, "mcrt_scatterer_create: NULL argument");
+  *out = nullptr;
+  if (d->kind != MCRT_RAYLEIGH && d->kind != MCRT_MIE)
+    return set_err(MCRT_EINVAL, "unknown scatterer kind");
+  if (!(d->kl > 0) || !std::isfinite(d->kl))
+    return set_err(MCRT_EINVAL, "scatterer mean free path kl must be positive");
+  std::unique_ptr<mcrt_scatterer> s(new mcrt_scatterer());
+  s->ctx = ctx;
+  s->kind = d->kind;
+  s->omega = d->omega;
+  s->kl = d->kl;
+  CK(cudaSetDevice(ctx->device));
+  if (d->kind == MCRT_MIE) {
+    if (d->n_theta < 2 || d->random_points < 1)
+      return set_err(MCRT_EINVAL, "Mie tables need n_theta >= 2 and random_points >= 1");
+    if (!d->F11 || !d->F12 || !d->F33 || !d->F34 || !d->S11 || !d->S22 || !d->csrn)
+      return set_err(MCRT_EINVAL, "Mie table pointer is NULL");
+    s->ntheta = d->n_theta;
+    s->rp = d->random_points;
+    const int nf = d->n_theta + 1;
+    std::vector<float4> F(nf, make_float4(0, 0, 0, 0)), S(nf, make_float4(0, 0, 0, 0));
+    for (int i = 0; i < d->n_theta; ++i) {
+      F[i] = make_float4((float)d->F11[i], (float)d->F12[i], (float)d->F33[i], (float)d->F34[i]);
+      S[i] = make_float4((float)d->S11[2 * i], (float)d->S11[2 * i + 1], (float)d->S22[2 * i],
+                         (float)d->S22[2 * i + 1]);
+    }
+    const int nc = ((d->random_points + 2 + 3) / 4) * 4;
+    std::vector<float> C(nc, 0.0f);
+    for (int i = 0; i <= d->random_points; ++i) C[i] = (float)d->csrn[i];
+    C[d->random_points + 1] = C[d->random_points];
+    CK(s->F.alloc(nf * sizeof(float4)));
+    CK(s->S.alloc(nf * sizeof(float4)));
+    CK(s->C.alloc(nc * sizeof(float)));
+    CK(cudaMemcpy(s->F.p, F.data(), nf * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->S.p, S.data(), nf * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->C.p, C.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  *out = s.release();
+  return MCRT_OK;
+}
+
+int mcrt_scatterer_destroy(mcrt_scatterer* s) {
+  if (!s) return MCRT_OK;
+  cudaSetDevice(s->ctx->device);
+  delete s;
+  return MCRT_OK;
+}
+
+int mcrt_mie_tables(double r, double m_re, double m_im, double lambda, double nu, int n_theta,
+                    int random_points, double* omega, double* kl, double* F11, double* F12,
+                    double* F33, double* F34, double* S11, double* S22, double* csrn, double* q) {
+  if (!(r > 0) || !(lambda > 0) || !(nu > 0) || n_theta < 2 || random_points < 1)
+    return set_err(MCRT_EINVAL, "mcrt_mie_tables: need r, lambda, nu > 0, n_theta >= 2, random_points >= 1");
+  const double x = 2 * host::PI * r / lambda;  // mie.jl:37
+  host::MieResult R = host::bhmie(x, host::cplx(m_re, m_im), n_theta);
+  if (omega) *omega = R.q_sca / R.q_ext;                   // mie.jl:39
+  if (kl) *kl = ((4.0 / 3.0) * r) / (nu * R.q_ext);        // mie.jl:40
+  for (int i = 0; i < n_theta; ++i) {
+    if (F11) F11[i] = R.F11[i];
+    if (F12) F12[i] = R.F12[i];
+    if (F33) F33[i] = R.F33[i];
+    if (F34) F34[i] = R.F34[i];
+    if (S11) {
+      S11[2 * i] = R.S1[i].real();
+      S11[2 * i + 1] = R.S1[i].imag();
+    }
+    if (S22) {
+      S22[2 * i] = R.S2[i].real();
+      S22[2 * i + 1] = R.S2[i].imag();
+    }
+  }
+  if (csrn) {
+    std::vector<double> c = host::calculate_csrn(R.F11, random_points);  // mie.jl:41-42
+    std::copy(c.begin(), c.end(), csrn);
+  }
+  if (q) {
+    q[0] = R.q_ext;
+    q[1] = R.q_sca;
+    q[2] = R.q_abs;
+    q[3] = R.q_back;
+    q[4] = R.asymm;
+  }
+  return MCRT_OK;
+}
+
+}  // extern "C"
+
+// ================================================================== validation
+namespace {
+
+constexpr double PI = host::PI;
+
+int validate_config(const mcrt_config* c, int geom) {
+  if (!c) return set_err(MCRT_EINVAL, "config is NULL");
+  if (c->number_of_rays < 0) return set_err(MCRT_EINVAL, "number_of_rays must be >= 0");
+  if (c->maximum_scattering_times < 0)
+    return set_err(MCRT_EINVAL, "maximum_scattering_times must be >= 0");
+  if (c->n_phi < 1 || c->n_theta < 1 || c->n_theta_b < 1 || c->n_phi_b < 1)
+    return set_err(MCRT_EINVAL, "bin counts must be >= 1");
+  if (geom == MCRT_PLANE && (c->n_theta % 2) != 0)
+    return set_err(MCRT_EINVAL, "a plane geometry needs an even Ntheta (two half-range quadratures)");
+  if (!c->cos_phi || !c->sin_phi || !c->cos_theta || !c->sin_theta || !c->inorm || !c->cos_theta_b ||
+      !c->sin_theta_b || !c->cos_phi_b || !c->sin_phi_b)
+    return set_err(MCRT_EINVAL, "config array pointer is NULL");
+  if (!(c->tau0 >= 0)) return set_err(MCRT_EINVAL, "tau0 must be >= 0");
+  return MCRT_OK;
+}
+
+// validate(p::PlaneGeometry) (plane.jl:52-62) and validate(s::SphereGeometry)
+// (sphere.jl:35-37), with the reference's messages.
+int validate_geometry(const mcrt_geometry* g) {
+  if (!g) return set_err(MCRT_EINVAL, "geometry is NULL");
+  if (g->kind == MCRT_PLANE) {
+    if (!(PI / 2 < g->theta && g->theta <= PI)) return set_err(MCRT_EINVAL, "θ must be in (π/2, π]");
+    if (!(0 <= g->phi && g->phi < 2 * PI)) return set_err(MCRT_EINVAL, "ϕ must be in [0, 2π)");
+    if (g->n_layers < 1 || !g->layers)
+      return set_err(MCRT_EINVAL, "There needs to be at least one layer");
+    if (g->n_layers > MAX_LAYERS) return set_err(MCRT_EINVAL, "too many layers (at most 8)");
+    for (int i = 0; i < g->n_layers; ++i) {
+      if (i != g->n_layers - 1 && g->layers[i].infinite)
+        return set_err(MCRT_EINVAL, "Only the last layer can be infinite");
+      if (!g->layers[i].scatterer) return set_err(MCRT_EINVAL, "layer scatterer is NULL");
+      if (!g->layers[i].infinite && !(g->layers[i].tau > 0))
+        return set_err(MCRT_EINVAL, "layer optical thickness must be positive");
+    }
+  } else if (g->kind == MCRT_SPHERE) {
+    if (g->n_layers != 1 || !g->layers || !g->layers[0].scatterer)
+      return set_err(MCRT_EINVAL, "a sphere has exactly one region with a scatterer");
+    if (!(g->layers[0].tau > 0)) return set_err(MCRT_EINVAL, "Radius must be positive");
+  } else {
+    return set_err(MCRT_EINVAL, "unknown geometry kind");
+  }
+  return MCRT_OK;
+}
+
+// ================================================================== bin tables
+struct HostBins {
+  std::vector<double> st, ct, g, w, cp, sp;
+  std::vector<double> kfx, kfy, kfz, ehx, ehy, gb, cf2, sf2, c1, c2, c3;
+  std::vector<int> upb;
+  std::vector<double> stb, ctb, cpb, spb;
+  int ntheta, nphi, nthetab, nphib, up0, up1, lo0, lo1;
+};
+
+// Per-bin constants of the RT grid (config.jl:78-99) and of the CB grid rotated into
+// the backscatter frame kfs (src/gpu.jl:92-94), including the CB bins' final rotation
+// into their own meridian planes (src/gpu.jl:127-133).
+HostBins make_bins(const mcrt_config* c, int geom, const host::Sph& kfs) {
+  HostBins H;
+  H.ntheta = c->n_theta;
+  H.nphi = c->n_phi;
+  H.nthetab = c->n_theta_b;
+  H.nphib = c->n_phi_b;
+  if (geom == MCRT_PLANE) {  // plane.jl:119,129
+    H.up0 = c->n_theta / 2;
+    H.up1 = c->n_theta;
+    H.lo0 = 0;
+    H.lo1 = c->n_theta / 2;
+  } else {  // sphere.jl:79,83
+    H.up0 = 0;
+    H.up1 = c->n_theta;
+    H.lo0 = 0;
+    H.lo1 = 0;
+  }
+  for (int j = 0; j < c->n_theta; ++j) {
+    H.st.push_back(c->sin_theta[j]);
+    H.ct.push_back(c->cos_theta[j]);
+    H.g.push_back(LOG2E_D / std::fabs(c->cos_theta[j]));
+    H.w.push_back(c->inorm[j]);
+  }
+  for (int j = 0; j < c->n_phi; ++j) {
+    H.cp.push_back(c->cos_phi[j]);
+    H.sp.push_back(c->sin_phi[j]);
+  }
+  for (int j = 0; j < c->n_theta_b; ++j) {
+    H.stb.push_back(c->sin_theta_b[j]);
+    H.ctb.push_back(c->cos_theta_b[j]);
+  }
+  for (int j = 0; j < c->n_phi_b; ++j) {
+    H.cpb.push_back(c->cos_phi_b[j]);
+    H.spb.push_back(c->sin_phi_b[j]);
+  }
+  for (int j2 = 0; j2 < c->n_phi_b; ++j2) {
+    for (int j1 = 0; j1 < c->n_theta_b; ++j1) {
+      const double stb = c->sin_theta_b[j1], ctb = c->cos_theta_b[j1];
+      const double cpb = c->cos_phi_b[j2], spb = c->sin_phi_b[j2];
+      host::V3 kf = host::ray_to_norm({stb * cpb, stb * spb, ctb}, kfs);
+      host::V3 Eh, Ev;
+      host::get_basis(kf, Eh, Ev);
+      host::V3 eh = host::norm_to_ray(Eh, kfs), ev = host::norm_to_ray(Ev, kfs);
+      const double cpsi = spb * eh.x - cpb * eh.y;
+      const double spsi = -spb * ev.x + cpb * ev.y;
+      H.kfx.push_back(kf.x);
+      H.kfy.push_back(kf.y);
+      H.kfz.push_back(kf.z);
+      H.ehx.push_back(Eh.x);
+      H.ehy.push_back(Eh.y);
+      H.gb.push_back(LOG2E_D / std::fabs(kf.z));
+      H.upb.push_back(kf.z > 0 ? 1 : 0);
+      H.cf2.push_back(cpsi * cpsi - spsi * spsi);
+      H.sf2.push_back(2.0 * cpsi * spsi);
+      H.c1.push_back(stb * cpb);
+      H.c2.push_back(stb * spb);
+      // cos(theta_b) - 1 without cancellation near the backscatter direction
+      H.c3.push_back(ctb > 0 ? -(stb * stb) / (1.0 + ctb) : ctb - 1.0);
+    }
+  }
+  return H;
+}
+
+struct Packer {
+  std::vector<unsigned char> bytes;
+  size_t add(const void* src, size_t n) {
+    size_t off = (bytes.size() + 255) & ~size_t(255);
+    bytes.resize(off + n);
+    std::memcpy(bytes.data() + off, src, n);
+    return off;
+  }
+};
+
+template <typename T>
+int upload_bins(const HostBins& H, DevBuf& buf) {
+  Packer P;
+  BinTables<T> hdr{};
+  P.add(&hdr, sizeof(hdr));
+  auto addv = [&](const std::vector<double>& v) {
+    std::vector<T> t(v.begin(), v.end());
+    if (t.empty()) t.push_back(T(0));
+    return P.add(t.data(), t.size() * sizeof(T));
+  };
+  size_t o_st = addv(H.st), o_ct = addv(H.ct), o_g = addv(H.g), o_w = addv(H.w), o_cp = addv(H.cp),
+         o_sp = addv(H.sp);
+  size_t o_kfx = addv(H.kfx), o_kfy = addv(H.kfy), o_kfz = addv(H.kfz), o_ehx = addv(H.ehx),
+         o_ehy = addv(H.ehy), o_gb = addv(H.gb), o_cf2 = addv(H.cf2), o_sf2 = addv(H.sf2),
+         o_c1 = addv(H.c1), o_c2 = addv(H.c2), o_c3 = addv(H.c3);
+  size_t o_upb = P.add(H.upb.data(), H.upb.size() * sizeof(int));
+  size_t o_stb = addv(H.stb), o_ctb = addv(H.ctb), o_cpb = addv(H.cpb), o_spb = addv(H.spb);
+  CK(buf.alloc(P.bytes.size()));
+  unsigned char* base = buf.as<unsigned char>();
+  hdr.ntheta = H.ntheta;
+  hdr.nphi = H.nphi;
+  hdr.nthetab = H.nthetab;
+  hdr.nphib = H.nphib;
+  hdr.up0 = H.up0;
+  hdr.up1 = H.up1;
+  hdr.lo0 = H.lo0;
+  hdr.lo1 = H.lo1;
+  auto at = [&](size_t o) { return reinterpret_cast<const T*>(base + o); };
+  hdr.st = at(o_st);
+  hdr.ct = at(o_ct);
+  hdr.g = at(o_g);
+  hdr.w = at(o_w);
+  hdr.cp = at(o_cp);
+  hdr.sp = at(o_sp);
+  hdr.kfx = at(o_kfx);
+  hdr.kfy = at(o_kfy);
+  hdr.kfz = at(o_kfz);
+  hdr.ehx = at(o_ehx);
+  hdr.ehy = at(o_ehy);
+  hdr.gb = at(o_gb);
+  hdr.cf2 = at(o_cf2);
+  hdr.sf2 = at(o_sf2);
+  hdr.c1 = at(o_c1);
+  hdr.c2 = at(o_c2);
+  hdr.c3 = at(o_c3);
+  hdr.upb = reinterpret_cast<const int*>(base + o_upb);
+  hdr.stb = at(o_stb);
+  hdr.ctb = at(o_ctb);
+  hdr.cpb = at(o_cpb);
+  hdr.spb = at(o_spb);
+  std::memcpy(P.bytes.data(), &hdr, sizeof(hdr));
+  CK(cudaMemcpy(buf.p, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
+  return MCRT_OK;
+}
+
+// Host copy of one instance: geometry, incidence frame, CB constants, RNG key.
+int make_instance(const mcrt_config* c, const mcrt_geometry* g, const double I0[4], uint64_t seed,
+                  uint32_t instance, int rng_mode, long long n_photons, long long photon_begin,
+                  DevInstance& D, host::Sph& kfs_out) {
+  std::memset(&D, 0, sizeof(D));
+  D.geom = g->kind;
+  D.n_layers = g->n_layers;
+  std::vector<const mcrt_scatterer*> sc;
+  for (int i = 0; i < g->n_layers; ++i) {
+    const mcrt_scatterer* s = g->layers[i].scatterer;
+    int k = -1;
+    for (size_t j = 0; j < sc.size(); ++j)
+      if (sc[j] == s) k = (int)j;
+    if (k < 0) {
+      if ((int)sc.size() >= MAX_SCAT) return set_err(MCRT_EINVAL, "at most 4 distinct scatterers");
+      sc.push_back(s);
+      k = (int)sc.size() - 1;
+    }
+    D.layers[i].tau = g->layers[i].tau;
+    D.layers[i].omega = g->layers[i].omega;
+    D.layers[i].inf = g->kind == MCRT_PLANE && g->layers[i].infinite ? 1 : 0;
+    D.layers[i].scat = k;
+  }
+  D.n_scat = (int)sc.size();
+  for (size_t j = 0; j < sc.size(); ++j) D.scat[j] = sc[j]->view();
+  double th0 = g->kind == MCRT_PLANE ? g->theta : PI, ph0 = g->kind == MCRT_PLANE ? g->phi : 0.0;
+  host::Sph inc{std::cos(th0), std::sin(th0), std::cos(ph0), std::sin(ph0)};
+  host::V3 k0 = host::ray_to_norm({0, 0, 1}, inc);  // MonteCarloRadiativeTransfer.jl:32
+  D.k0[0] = k0.x;
+  D.k0[1] = k0.y;
+  D.k0[2] = k0.z;
+  D.inc[0] = inc.ct;
+  D.inc[1] = inc.st;
+  D.inc[2] = inc.cp;
+  D.inc[3] = inc.sp;
+  for (int s = 0; s < 4; ++s) D.I0[s] = I0[s];
+  host::E_from_I(I0, D.Ei);
+  host::V3 kf{-k0.x, -k0.y, -k0.z};  // kf = -kpath[1] (src/gpu.jl:48)
+  host::Sph kfs = host::spherical(kf);
+  kfs_out = kfs;
+  D.kfs[0] = kfs.ct;
+  D.kfs[1] = kfs.st;
+  D.kfs[2] = kfs.cp;
+  D.kfs[3] = kfs.sp;
+  D.kf0[0] = kf.x;
+  D.kf0[1] = kf.y;
+  D.kf0[2] = kf.z;
+  host::V3 Eh, Ev;
+  host::get_basis(kf, Eh, Ev);
+  D.eh0[0] = Eh.x;
+  D.eh0[1] = Eh.y;
+  // rows of norm_to_ray for the frame kfs
+  D.Rkfs[0] = kfs.ct * kfs.cp;
+  D.Rkfs[1] = kfs.ct * kfs.sp;
+  D.Rkfs[2] = -kfs.st;
+  D.Rkfs[3] = -kfs.sp;
+  D.Rkfs[4] = kfs.cp;
+  D.Rkfs[5] = 0.0;
+  D.Rkfs[6] = kfs.st * kfs.cp;
+  D.Rkfs[7] = kfs.st * kfs.sp;
+  D.Rkfs[8] = kfs.ct;
+  D.kl1 = g->layers[0].scatterer->kl;  // mean_free_path(g, 1) (src/gpu.jl:102)
+  D.min_int = c->minimum_intensity;
+  D.tau0 = c->tau0;
+  D.max_scat = c->maximum_scattering_times;
+  D.compute_cb = c->compute_cb ? 1 : 0;
+  D.n_photons = n_photons;
+  D.photon_begin = photon_begin;
+  D.nrays = c->number_of_rays > 0 ? c->number_of_rays : 1;
+  D.key0 = (unsigned)seed;
+  D.key1 = (unsigned)(seed >> 32) + 0x632BE5ABu * instance;
+  D.rng_mode = rng_mode;
+  return MCRT_OK;
+}
+
+// ================================================================== kernel dispatch
+bool kernel_info(int prec, int bs, KInfo& k) {
+  return prec == MCRT_FP32 ? kernel_info_fp32(bs, k) : kernel_info_fp64(bs, k);
+}
+
+int table_f4_of(const DevInstance& D) {
+  int f4 = 0;
+  for (int s = 0; s < D.n_scat; ++s)
+    if (D.scat[s].kind == 1) f4 += 2 * (D.scat[s].ntheta + 1) + (D.scat[s].rp + 2 + 3) / 4;
+  return f4;
+}
+
+}  // namespace
+
+// ================================================================== launches
+struct Launch {
+  int precision = MCRT_FP32, kernel = MCRT_KERNEL_PERSISTENT;
+  int bs = 256, bpsm = 0, blocks = 0;
+  size_t smem = 0;
+  int table_f4 = 0;
+};
+
+// Everything a group of instances needs on the device: descriptors, bin tables,
+// tallies, counters and the photon-state pool.
+struct Group {
+  mcrt_ctx* ctx = nullptr;
+  Launch L;
+  int n_inst = 0;
+  std::vector<DevInstance> hinst;   // host copies (device pointers filled in)
+  std::vector<int> order;           // device slot -> user index
+  std::vector<std::unique_ptr<DevBuf>> bins;
+  DevBuf d_inst, d_tally, d_claim, d_status, d_state, d_tacc;
+  DevBuf d_kpath, d_xpath, d_idx;  // plain kernel path history
+  long long plain_threads = 0;
+  size_t nrt = 0, ncb = 0, per_inst = 0;  // tally doubles per instance
+  float last_ms = 0.f;
+  double photons = 0;
+};
+
+namespace {
+
+int size_launch(mcrt_ctx* ctx, Group& G, const mcrt_run_opts* o, const std::string& sig) {
+  Launch& L = G.L;
+  L.precision = o ? o->precision : MCRT_FP32;
+  L.kernel = o ? o->kernel : MCRT_KERNEL_PERSISTENT;
+  if (L.precision != MCRT_FP32 && L.precision != MCRT_FP64)
+    return set_err(MCRT_EINVAL, "precision must be MCRT_FP32 or MCRT_FP64");
+  if (L.kernel != MCRT_KERNEL_PERSISTENT && L.kernel != MCRT_KERNEL_PLAIN)
+    return set_err(MCRT_EINVAL, "unknown kernel kind");
+  if (L.kernel == MCRT_KERNEL_PLAIN) return MCRT_OK;
+  int bs = o && o->block_size ? o->block_size : 0;
+  int bpsm = o && o->blocks_per_sm ? o->blocks_per_sm : 0;
+  if (!bs) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->tuned.find(sig);
+    if (it != ctx->tuned.end()) {
+      bs = it->second.first;
+      if (!bpsm) bpsm = it->second.second;
+    }
+  }
+  if (!bs) bs = L.precision == MCRT_FP32 ? 256 : 128;
+  KInfo ki;
+  if (!kernel_info(L.precision, bs, ki))
+    return set_err(MCRT_EINVAL, "unsupported block size for this precision (FP32: 128/256/512, FP64: 128/256)");
+  int tf4 = 0;
+  for (auto& D : G.hinst) tf4 = std::max(tf4, table_f4_of(D));
+  size_t smem = ki.shared_static + (size_t)tf4 * 16;
+  if (smem > (size_t)ctx->smem_optin) {
+    // the tables that do not fit are read from global memory through L1
+    tf4 = (int)((ctx->smem_optin - ki.shared_static) / 16);
+    if (tf4 < 0) return set_err(MCRT_EINVAL, "block size too large for shared memory");
+    smem = ki.shared_static + (size_t)tf4 * 16;
+  }
+  CK(cudaFuncSetAttribute(ki.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ki.fn, bs, smem));
+  if (occ < 1) return set_err(MCRT_EINVAL, "kernel does not fit on an SM with this block size");
+  if (!bpsm || bpsm > occ) bpsm = occ;
+  L.bs = bs;
+  L.bpsm = bpsm;
+  L.blocks = ctx->sms * bpsm;
+  L.smem = smem;
+  L.table_f4 = tf4;
+  return MCRT_OK;
+}
+
+// Allocates tallies, counters, bins and state for the group's instances.
+int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const* geoms,
+                const double (*I0)[4], const uint64_t* seeds, const uint32_t* insts,
+                const long long* nph, long long photon_begin, int rng_mode, int n,
+                const mcrt_run_opts* o, Group& G) {
+  G.ctx = ctx;
+  G.n_inst = n;
+  G.hinst.resize(n);
+  std::vector<host::Sph> kfs(n);
+  for (int i = 0; i < n; ++i) {
+    int rc = make_instance(c, geoms[i], I0[i], seeds[i], insts[i], rng_mode, nph[i], photon_begin,
+                           G.hinst[i], kfs[i]);
+    if (rc) return rc;
+  }
+  // order instances by photon budget, largest first (blocks walk the list in order)
+  G.order.resize(n);
+  for (int i = 0; i < n; ++i) G.order[i] = i;
+  std::stable_sort(G.order.begin(), G.order.end(),
+                   [&](int a, int b) { return G.hinst[a].n_photons > G.hinst[b].n_photons; });
+  std::string sig = std::to_string(geoms[0]->kind) + "/" + std::to_string(c->n_theta) + "x" +
+                    std::to_string(c->n_phi) + "/" + std::to_string(c->n_theta_b) + "x" +
+                    std::to_string(c->n_phi_b) + "/" + std::to_string(G.hinst[0].scat[0].kind) +
+                    "/" + std::to_string(o ? o->precision : 0);
+  int rc = size_launch(ctx, G, o, sig);
+  if (rc) return rc;
+  // bin tables, one per distinct (geometry kind, incidence)
+  std::map<std::string, const void*> bin_cache;
+  for (int i = 0; i < n; ++i) {
+    char key[128];
+    std::snprintf(key, sizeof key, "%d/%.17g/%.17g/%.17g/%.17g", geoms[i]->kind, kfs[i].ct, kfs[i].st,
+                  kfs[i].cp, kfs[i].sp);
+    auto it = bin_cache.find(key);
+    if (it == bin_cache.end()) {
+      HostBins H = make_bins(c, geoms[i]->kind, kfs[i]);
+      std::unique_ptr<DevBuf> b(new DevBuf());
+      rc = G.L.precision == MCRT_FP32 ? upload_bins<float>(H, *b) : upload_bins<double>(H, *b);
+      if (rc) return rc;
+      bin_cache[key] = b->p;
+      G.bins.push_back(std::move(b));
+      it = bin_cache.find(key);
+    }
+    G.hinst[i].bins = it->second;
+  }
+  G.nrt = 4 * (size_t)c->n_theta * c->n_phi;
+  G.ncb = 4 * (size_t)c->n_theta_b * c->n_phi_b;
+  G.per_inst = G.nrt + G.ncb + G.ncb / 4 + NACC;
+  CK(G.d_tally.alloc(G.per_inst * n * sizeof(double)));
+  CK(G.d_claim.alloc(n * sizeof(unsigned long long)));
+  CK(G.d_status.alloc(sizeof(unsigned)));
+  for (int i = 0; i < n; ++i) {
+    double* base = G.d_tally.as<double>() + G.per_inst * i;
+    G.hinst[i].Irt = base;
+    G.hinst[i].Icb = base + G.nrt;
+    G.hinst[i].ladder = base + G.nrt + G.ncb;
+    G.hinst[i].acc = base + G.nrt + G.ncb + G.ncb / 4;
+    G.hinst[i].claim = G.d_claim.as<unsigned long long>() + i;
+  }
+  std::vector<DevInstance> dev(n);
+  for (int s = 0; s < n; ++s) dev[s] = G.hinst[G.order[s]];
+  CK(G.d_inst.alloc(n * sizeof(DevInstance)));
+  CK(cudaMemcpy(G.d_inst.p, dev.data(), n * sizeof(DevInstance), cudaMemcpyHostToDevice));
+  if (G.L.kernel == MCRT_KERNEL_PERSISTENT) {
+    KInfo ki;
+    kernel_info(G.L.precision, G.L.bs, ki);
+    size_t slots = (size_t)G.L.blocks * G.L.bs;
+    CK(G.d_state.alloc(slots * ki.state_bytes));
+    CK(G.d_tacc.alloc(slots * NACC * sizeof(double)));
+  } else {
+    if (n != 1) return set_err(MCRT_EINVAL, "the plain kernel runs one instance per launch");
+    long long th = o && o->plain_threads > 0 ? o->plain_threads
+                                             : std::min<long long>(c->maximum_threads > 0 ? c->maximum_threads : 8192,
+                                                                   std::max<long long>(nph[0], 1));
+    G.plain_threads = th;
+    size_t rows = (size_t)c->maximum_scattering_times + 1;
+    size_t vb = G.L.precision == MCRT_FP32 ? 3 * sizeof(float) : 3 * sizeof(double);
+    CK(G.d_kpath.alloc(rows * th * vb));
+    CK(G.d_xpath.alloc(rows * th * vb));
+    CK(G.d_idx.alloc(rows * th * sizeof(int)));
+  }
+  return MCRT_OK;
+}
+
+int launch_group(Group& G) {
+  mcrt_ctx* ctx = G.ctx;
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemsetAsync(G.d_tally.p, 0, G.d_tally.n, st));
+  CK(cudaMemsetAsync(G.d_claim.p, 0, G.d_claim.n, st));
+  CK(cudaMemsetAsync(G.d_status.p, 0, G.d_status.n, st));
+  G.photons = 0;
+  for (auto& D : G.hinst) G.photons += (double)D.n_photons;
+  CK(cudaEventRecord(ctx->e0, st));
+  if (G.L.kernel == MCRT_KERNEL_PERSISTENT) {
+    KInfo ki;
+    kernel_info(G.L.precision, G.L.bs, ki);
+    KParams p;
+    p.inst = G.d_inst.as<const DevInstance>();
+    p.n_inst = G.n_inst;
+    p.state = G.d_state.as<uint4>();
+    p.tacc = G.d_tacc.as<double>();
+    p.status = G.d_status.as<unsigned>();
+    p.table_f4 = G.L.table_f4;
+    CK(launch_transport(ki, G.L.blocks, G.L.bs, G.L.smem, st, p));
+  } else {
+    PlainParams p;
+    p.inst = G.d_inst.as<const DevInstance>();
+    p.kpath = G.d_kpath.as<double>();
+    p.xpath = G.d_xpath.as<double>();
+    p.idxpath = G.d_idx.as<int>();
+    p.threads = G.plain_threads;
+    p.maxord = (long long)(G.d_idx.n / sizeof(int) / std::max<long long>(G.plain_threads, 1));
+    p.status = G.d_status.as<unsigned>();
+    int blocks = (int)((G.plain_threads + 255) / 256);
+    CK(launch_plain(G.L.precision == MCRT_FP64, blocks, st, p));
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->e1, st));
+  return MCRT_OK;
+}
+
+int finish_group(Group& G) {
+  CK(cudaEventSynchronize(G.ctx->e1));
+  CK(cudaEventElapsedTime(&G.last_ms, G.ctx->e0, G.ctx->e1));
+  return MCRT_OK;
+}
+
+int read_instance(Group& G, int user_index, double A_out[5], double* Irt, double* Icb, double* lad,
+                  mcrt_stats* stats) {
+  CK(cudaStreamSynchronize(G.ctx->stream));
+  std::vector<double> h(G.per_inst);
+  const double* src = G.hinst[user_index].Irt;
+  CK(cudaMemcpy(h.data(), src, G.per_inst * sizeof(double), cudaMemcpyDeviceToHost));
+  unsigned status = 0;
+  CK(cudaMemcpy(&status, G.d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  const double* acc = h.data() + G.nrt + G.ncb + G.ncb / 4;
+  if (A_out)
+    for (int s = 0; s < 5; ++s) A_out[s] = acc[s];
+  if (Irt) std::memcpy(Irt, h.data(), G.nrt * sizeof(double));
+  if (Icb) std::memcpy(Icb, h.data() + G.nrt, G.ncb * sizeof(double));
+  if (lad) std::memcpy(lad, h.data() + G.nrt + G.ncb, G.ncb / 4 * sizeof(double));
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->cb_peak_sum = acc[ACC_PEAK];
+    stats->cb_peak_sumsq = acc[ACC_PEAK2];
+    stats->photons = acc[ACC_PHOTONS];
+    stats->events = acc[ACC_EVENTS];
+    stats->attempts = acc[ACC_ATTEMPTS];
+    stats->rt_evals = acc[ACC_RT];
+    stats->cb1_evals = acc[ACC_CB1];
+    stats->cbn_evals = acc[ACC_CBN];
+    stats->kernel_ms = G.last_ms;
+    stats->status_flags = (int)status;
+    stats->block_size = G.L.kernel == MCRT_KERNEL_PERSISTENT ? G.L.bs : 256;
+    stats->blocks = G.L.kernel == MCRT_KERNEL_PERSISTENT ? G.L.blocks : (int)((G.plain_threads + 255) / 256);
+  }
+  return MCRT_OK;
+}
+
+}  // namespace
+
+// ================================================================== public entry points
+struct mcrt_solve {
+  Group G;
+};
+struct mcrt_batch {
+  Group G;
+};
+
+extern "C" {
+
+int mcrt_solve_create(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g,
+                      const double I0[4], const mcrt_run_opts* opts, mcrt_solve** out) {
+  if (!ctx || !out || !I0) return set_err(MCRT_EINVAL, "mcrt_solve_create: NULL argument");
+  *out = nullptr;
+  int rc = validate_geometry(g);
+  if (rc) return rc;
+  rc = validate_config(cfg, g->kind);
+  if (rc) return rc;
+  CK(cudaSetDevice(ctx->device));
+  std::unique_ptr<mcrt_solve> s(new mcrt_solve());
+  const mcrt_geometry* gs[1] = {g};
+  double I[1][4] = {{I0[0], I0[1], I0[2], I0[3]}};
+  uint64_t seed = opts ? opts->seed : 0;
+  uint32_t inst = opts ? opts->instance : 0;
+  long long nph = cfg->number_of_rays;
+  rc = build_group(ctx, cfg, gs, I, &seed, &inst, &nph, opts ? opts->photon_begin : 0,
+                   opts ? opts->rng_mode : 0, 1, opts, s->G);
+  if (rc) return rc;
+  *out = s.release();
+  return MCRT_OK;
+}
+
+int mcrt_solve_launch(mcrt_solve* s, int64_t photon_begin, int64_t n_photons) {
+  if (!s || n_photons < 0) return set_err(MCRT_EINVAL, "mcrt_solve_launch: bad argument");
+  DevInstance& D = s->G.hinst[0];
+  if (D.n_photons != n_photons || D.photon_begin != photon_begin) {
+    D.n_photons = n_photons;
+    D.photon_begin = photon_begin;
+    CK(cudaMemcpyAsync(s->G.d_inst.p, &D, sizeof(DevInstance), cudaMemcpyHostToDevice, s->G.ctx->stream));
+    CK(cudaStreamSynchronize(s->G.ctx->stream));
+  }
+  return launch_group(s->G);
+}
+
+int mcrt_solve_read(mcrt_solve* s, double A_out[5], double* Irt, double* Icb, double* Icb_ladder,
+                    mcrt_stats* stats) {
+  if (!s) return set_err(MCRT_EINVAL, "mcrt_solve_read: NULL solve");
+  int rc = finish_group(s->G);
+  if (rc) return rc;
+  return read_instance(s->G, 0, A_out, Irt, Icb, Icb_ladder, stats);
+}
+
+int mcrt_solve_destroy(mcrt_solve* s) {
+  if (!s) return MCRT_OK;
+  cudaSetDevice(s->G.ctx->device);
+  cudaStreamSynchronize(s->G.ctx->stream);
+  delete s;
+  return MCRT_OK;
+}
+
+int mcrt_simulate(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g, const double I0[4],
+                  const mcrt_run_opts* opts, double A_out[5], double* Irt, double* Icb,
+                  double* Icb_ladder, mcrt_stats* stats) {
+  if (!A_out || !Irt || !Icb) return set_err(MCRT_EINVAL, "mcrt_simulate: output pointer is NULL");
+  mcrt_solve* s = nullptr;
+  int rc = mcrt_solve_create(ctx, cfg, g, I0, opts, &s);
+  if (rc) return rc;
+  std::unique_ptr<mcrt_solve, int (*)(mcrt_solve*)> guard(s, mcrt_solve_destroy);
+  rc = mcrt_solve_launch(s, opts ? opts->photon_begin : 0, cfg->number_of_rays);
+  if (rc) return rc;
+  rc = mcrt_solve_read(s, A_out, Irt, Icb, Icb_ladder, stats);
+  if (rc) return rc;
+  // divide by the number of rays (MonteCarloRadiativeTransfer.jl:78-84)
+  const double inv = cfg->number_of_rays > 0 ? 1.0 / (double)cfg->number_of_rays : 0.0;
+  for (int i = 0; i < 5; ++i) A_out[i] *= inv;
+  for (size_t i = 0; i < s->G.nrt; ++i) Irt[i] *= inv;
+  for (size_t i = 0; i < s->G.ncb; ++i) Icb[i] *= inv;
+  if (Icb_ladder)
+    for (size_t i = 0; i < s->G.ncb / 4; ++i) Icb_ladder[i] *= inv;
+  if (stats && (stats->status_flags & MCRT_FLAG_REJECT_LIMIT))
+    return set_err(MCRT_ENONCONV, "a rejection loop hit its iteration cap; see stats.status_flags");
+  return MCRT_OK;
+}
+
+int mcrt_batch_create(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_instance* inst, int n_inst,
+                      const mcrt_run_opts* opts, mcrt_batch** out) {
+  if (!ctx || !inst || !out || n_inst < 1) return set_err(MCRT_EINVAL, "mcrt_batch_create: bad argument");
+  *out = nullptr;
+  if (opts && opts->kernel == MCRT_KERNEL_PLAIN)
+    return set_err(MCRT_EINVAL, "batches run on the persistent kernel");
+  std::vector<const mcrt_geometry*> gs(n_inst);
+  std::vector<double> I(4 * (size_t)n_inst);
+  std::vector<uint64_t> seeds(n_inst);
+  std::vector<uint32_t> ids(n_inst);
+  std::vector<long long> nph(n_inst);
+  for (int i = 0; i < n_inst; ++i) {
+    int rc = validate_geometry(inst[i].geometry);
+    if (rc) return rc;
+    rc = validate_config(cfg, inst[i].geometry->kind);
+    if (rc) return rc;
+    if (inst[i].n_photons < 0) return set_err(MCRT_EINVAL, "n_photons must be >= 0");
+    gs[i] = inst[i].geometry;
+    for (int s = 0; s < 4; ++s) I[4 * i + s] = inst[i].I0[s];
+    seeds[i] = inst[i].seed;
+    ids[i] = inst[i].instance;
+    nph[i] = inst[i].n_photons;
+  }
+  CK(cudaSetDevice(ctx->device));
+  std::unique_ptr<mcrt_batch> b(new mcrt_batch());
+  int rc = build_group(ctx, cfg, gs.data(), reinterpret_cast<const double(*)[4]>(I.data()), seeds.data(),
+                       ids.data(), nph.data(), 0, opts ? opts->rng_mode : 0, n_inst, opts, b->G);
+  if (rc) return rc;
+  *out = b.release();
+  return MCRT_OK;
+}
+
+int mcrt_batch_launch(mcrt_batch* b) {
+  if (!b) return set_err(MCRT_EINVAL, "mcrt_batch_launch: NULL batch");
+  return launch_group(b->G);
+}
+
+int mcrt_batch_read(mcrt_batch* b, int i, double A_out[5], double* Irt, double* Icb, double* lad,
+                    mcrt_stats* stats) {
+  if (!b || i < 0 || i >= b->G.n_inst) return set_err(MCRT_EINVAL, "mcrt_batch_read: bad index");
+  int rc = finish_group(b->G);
+  if (rc) return rc;
+  return read_instance(b->G, i, A_out, Irt, Icb, lad, stats);
+}
+
+int mcrt_batch_timing(mcrt_batch* b, double* kernel_ms, double* photons) {
+  if (!b) return set_err(MCRT_EINVAL, "mcrt_batch_timing: NULL batch");
+  int rc = finish_group(b->G);
+  if (rc) return rc;
+  if (kernel_ms) *kernel_ms = b->G.last_ms;
+  if (photons) *photons = b->G.photons;
+  return MCRT_OK;
+}
+
+int mcrt_batch_destroy(mcrt_batch* b) {
+  if (!b) return MCRT_OK;
+  cudaSetDevice(b->G.ctx->device);
+  cudaStreamSynchronize(b->G.ctx->stream);
+  delete b;
+  return MCRT_OK;
+}
+
+}  // extern "C"
+
+// ================================================================== FP32 peak
+namespace {
+// Eight independent FMA chains per thread; the result is stored only if it is
+// impossible, so nothing is elided.
+__global__ void k_fma_peak(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+        x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      x0 = fmaf(x0, a, b);
+      x1 = fmaf(x1, a, b);
+      x2 = fmaf(x2, a, b);
+      x3 = fmaf(x3, a, b);
+      x4 = fmaf(x4, a, b);
+      x5 = fmaf(x5, a, b);
+      x6 = fmaf(x6, a, b);
+      x7 = fmaf(x7, a, b);
+    }
+  }
+  float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == -1.2345f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" int mcrt_measure_fp32_peak(mcrt_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return set_err(MCRT_EINVAL, "mcrt_measure_fp32_peak: NULL argument");
+  CK(cudaSetDevice(ctx->device));
+  DevBuf out;
+  const int threads = 256, blocks = ctx->sms * 8, iters = 4096;
+  CK(out.alloc((size_t)threads * blocks * sizeof(float)));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    CK(cudaEventRecord(ctx->e0, ctx->stream));
+    k_fma_peak<<<blocks, threads, 0, ctx->stream>>>(out.as<float>(), iters, 0.9999f, 0.0001f);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->e1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->e0, ctx->e1));
+    if (rep > 0) best = std::min(best, ms);
+  }
+  const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return MCRT_OK;
+}

@@ -1,0 +1,978 @@
+// Persistent event-batched transport kernel.
+//
+// Replaces the reference's per-ray gpu_kernel (MonteCarloRadiativeTransfer.jl
+// src/gpu.jl:177-296) with the same physics organised for sm_103a:
+//
+//  * One thread owns one photon path at a time and, in a *sample* phase, advances it
+//    by one scattering event: Philox draws, scatter(), the free-path rejection loop,
+//    absorption, and the incremental reciprocal-path (CB) state (src/gpu.jl:207-260).
+//    The event's parameters go to shared memory.
+//  * In the *collect* phase the whole block sweeps the peel-off bins. Lanes own bins,
+//    not photons: a warp takes a tile of 32 x NB bins (RT: one azimuth and NB polar
+//    angles per lane; CB: one bin pair per lane) and loops over every event of the
+//    batch, reading the event (a shared-memory broadcast) and accumulating the bins'
+//    Stokes contributions in registers. This is src/gpu.jl:6-34 (RT) and :41-175 (CB)
+//    with the event loop and the bin loop exchanged, so tallies need no atomics per
+//    contribution: each lane flushes its bins once per batch with FP64 reductions.
+//    The per-event escaped intensity (the return value of collect_rt_gpu!) is summed
+//    with __shfl_xor_sync across the warp and added per warp into shared memory.
+//  * The *finish* phase renormalises each photon by its escaped intensity
+//    (src/gpu.jl:288-291), ends finished paths and claims new photons from the
+//    instance's work queue (a global counter, claimed warp-aggregated).
+//
+// Work: one launch serves any number of instances (simulate() calls); a block works on
+// one instance at a time and moves to the next when the current one has no photons
+// left to claim, so uneven batches run in one persistent launch.
+#pragma once
+
+#include "mcrt_device.cuh"
+
+namespace mcrt {
+
+constexpr int EV_UP = 1, EV_DN = 2, EV_CB = 4, EV_CBN = 8;
+constexpr unsigned MAX_ATTEMPTS = 1u << 20;
+
+template <typename T>
+struct __align__(16) EventP {
+  T I[4];                 // Stokes after absorption
+  T fct, fst, fcp, fsp;   // spherical frame of the incoming direction (ka)
+  T a_up, a_dn;           // plane: distance numerators of xa (up: -z, down: z + tau)
+  T xax, xay, xaz, Da;    // sphere: xa and tau^2 - |xa|^2
+  T bct, bst, bcp, bsp;   // CB: frame of kb = -k_2
+  T ea[4], eb[4];         // CB: reciprocal-path fields at xa and xb
+  T b_up, b_dn, tab2;     // CB: distance numerators of xb; (tau_a - tau_b) * log2(e)
+  T v1, v2, v3;           // CB: phase coefficients, kl (xa - xb) in the backscatter frame / 2 pi
+  T xbx, xby, xbz, Db;    // CB sphere: xb and tau^2 - |xb|^2
+  int flags, layer, pad0, pad1;
+};
+
+template <typename T>
+struct __align__(16) PState {
+  double x[3], x1[3];
+  double logA, logL, peak;
+  unsigned long long id;
+  T I[4];
+  T k[3], wI;
+  T Ih[4];
+  T k2[3], pad0;
+  T kprev[3], pad1;
+  T A[4];
+  T L[8];
+  int n, idx, idx1, pad2;
+};
+
+template <typename T, int BS>
+struct __align__(16) Shared {
+  DevInstance inst;
+  EventP<T> ev[BS];
+  T esc_up[BS], esc_dn[BS], peak[BS];
+  unsigned short list[4][BS];  // 0 up, 1 down, 2 CB order > 1, 3 CB order 1
+  int cnt[2][4];
+  int item_next;
+  int cur;
+  int exhausted;
+  int pad;
+};
+
+struct KParams {
+  const DevInstance* inst;
+  int n_inst;
+  uint4* state;          // photon state pool, SoA of 16-byte words
+  double* tacc;          // per-thread accumulators, SoA [NACC][slots]
+  unsigned* status;      // status flags (mcrt_status_flags)
+  int table_f4;          // shared-memory table capacity in float4
+};
+
+template <typename T>
+__device__ __forceinline__ void ps_load(PState<T>& s, const uint4* base, size_t stride, size_t g) {
+  constexpr int N = sizeof(PState<T>) / 16;
+  union U {
+    PState<T> p;
+    uint4 q[N];
+    __device__ U() {}
+  } u;
+#pragma unroll
+  for (int i = 0; i < N; ++i) u.q[i] = base[(size_t)i * stride + g];
+  s = u.p;
+}
+
+template <typename T>
+__device__ __forceinline__ void ps_store(const PState<T>& s, uint4* base, size_t stride, size_t g) {
+  constexpr int N = sizeof(PState<T>) / 16;
+  union U {
+    PState<T> p;
+    uint4 q[N];
+    __device__ U() {}
+  } u;
+  u.p = s;
+#pragma unroll
+  for (int i = 0; i < N; ++i) base[(size_t)i * stride + g] = u.q[i];
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sphere distance to the boundary along a unit direction with k.x = kx and
+// D = tau^2 - |x|^2 >= 0, in a cancellation-free form of sphere.jl:69-73.
+template <typename T>
+__device__ __forceinline__ T sphere_t(T kx, T D) {
+  T r = MT<T>::sqrt(kx * kx + D);
+  return kx > T(0) ? D / (kx + r) : r - kx;
+}
+
+// ------------------------------------------------------------------ instance staging
+// Copies the instance into shared memory and stages its Mie tables there with
+// coalesced 16-byte loads; the shared copy's table pointers are redirected.
+template <typename T, int BS>
+__device__ void stage_instance(Shared<T, BS>& sh, float4* tables, const KParams& p, int cur) {
+  const int tid = threadIdx.x;
+  {
+    const int4* src = reinterpret_cast<const int4*>(&p.inst[cur]);
+    int4* dst = reinterpret_cast<int4*>(&sh.inst);
+    constexpr int N = sizeof(DevInstance) / 16;
+    for (int i = tid; i < N; i += BS) dst[i] = src[i];
+  }
+  __syncthreads();
+  int off = 0;
+  const DevInstance& src = p.inst[cur];
+  for (int s = 0; s < src.n_scat; ++s) {
+    const DevScatterer& d = src.scat[s];
+    if (d.kind != 1) continue;
+    int nf = d.ntheta + 1;
+    int nc4 = (d.rp + 2 + 3) / 4;
+    if (off + 2 * nf + nc4 > p.table_f4) continue;  // stays in global memory (L1/L2)
+    float4* F = tables + off;
+    float4* S = F + nf;
+    float4* C = S + nf;
+    for (int i = tid; i < nf; i += BS) {
+      F[i] = d.F[i];
+      S[i] = d.S[i];
+    }
+    const float4* c4 = reinterpret_cast<const float4*>(d.csrn);
+    for (int i = tid; i < nc4; i += BS) C[i] = c4[i];
+    if (tid == 0) {
+      sh.inst.scat[s].F = F;
+      sh.inst.scat[s].S = S;
+      sh.inst.scat[s].csrn = reinterpret_cast<const float*>(C);
+    }
+    off += 2 * nf + nc4;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int next_instance(const KParams& p, int cur) {
+  for (int i = cur + 1; i < p.n_inst; ++i) {
+    unsigned long long c = atomicAdd(p.inst[i].claim, 0ull);
+    if ((long long)c < p.inst[i].n_photons) return i;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void acc_add(double* tacc, size_t stride, size_t g, int k, double v) {
+  tacc[(size_t)k * stride + g] += v;
+}
+
+// ------------------------------------------------------------------ photon start
+// Start of cpu_kernel / gpu_kernel for one photon: initial_x, direct transmission and
+// initial_propagation (src/gpu.jl:187-204; plane.jl:64-95; sphere.jl:39-67), in FP64.
+template <typename T>
+__device__ bool start_photon(PState<T>& ps, const DevInstance& in, unsigned long long ph,
+                             double* tacc, size_t stride, size_t g, unsigned* status) {
+  ps.id = ph;
+  ps.n = 0;
+  ps.idx = 0;
+  ps.idx1 = 0;
+  ps.peak = 0.0;
+  double I[4] = {in.I0[0], in.I0[1], in.I0[2], in.I0[3]};
+  double k[3] = {in.k0[0], in.k0[1], in.k0[2]};
+  double x[3] = {0.0, 0.0, 0.0};
+  Draw d0 = draw(in.key0, in.key1, ph, 0, 0);
+  double tau1 = in.layers[0].tau;
+  if (in.geom == 1) {
+    double r = tau1 * sqrt(u01<double>(d0.r[0]));
+    double phi = 2 * PI_D * u01<double>(d0.r[1]);
+    double s, c;
+    sincos(phi, &s, &c);
+    x[0] = r * c;
+    x[1] = r * s;
+    x[2] = sqrt(tau1 * tau1 - r * r);
+  }
+  bool cdt = in.geom == 1 || (in.n_layers == 1 && !in.layers[0].inf);
+  if (cdt) {
+    double tp = dist_d(in, x, k[0], k[1], k[2], 0);
+    double dt = tp <= in.tau0 ? exp(-tp) : 0.0;
+    acc_add(tacc, stride, g, ACC_ADT, I[0] * dt);
+    for (int s = 0; s < 4; ++s) I[s] *= 1 - dt;
+  }
+  double u2 = in.rng_mode == 1 ? ((double)ph + 0.5) / (double)in.nrays : u01<double>(d0.r[2]);
+  double t;
+  if (in.geom == 0) {
+    if (in.layers[0].inf) {
+      t = -log(u2);
+    } else {
+      double tp = dist_d(in, x, k[0], k[1], k[2], 0);
+      if (cdt && tp <= in.tau0) {
+        t = -log(1 - u2 * (1 - exp(-tp)));
+      } else {
+        t = tp + 1;
+        for (unsigned a = 0; t > tp; ++a) {
+          if (a >= MAX_ATTEMPTS) {
+            atomicOr(status, 1u);
+            acc_add(tacc, stride, g, ACC_REJECT_CAP, 1.0);
+            t = tp;
+            break;
+          }
+          double u = a == 0 ? u2 : u01<double>(draw(in.key0, in.key1, ph, 0, a).r[2]);
+          t = -log(u);
+        }
+      }
+    }
+  } else {
+    double tp = 2.0 * x[2];
+    if (tp <= in.tau0) {
+      t = -log(1 - u2 * (1 - exp(-tp)));
+    } else {
+      t = tp + 1;
+      for (unsigned a = 0; t > tp; ++a) {
+        if (a >= MAX_ATTEMPTS) {
+          atomicOr(status, 1u);
+          acc_add(tacc, stride, g, ACC_REJECT_CAP, 1.0);
+          t = tp;
+          break;
+        }
+        uint32_t r = a == 0 ? d0.r[2] : draw(in.key0, in.key1, ph, 0, a).r[2];
+        double uc = in.rng_mode == 1 && a == 0 ? 1.0 - u2 : u01<double>(~r);  // 1 - u (sphere.jl:61)
+        t = -log(uc);
+      }
+    }
+  }
+  for (int s = 0; s < 3; ++s) {
+    ps.x[s] = x[s] + t * k[s];
+    ps.k[s] = (T)k[s];
+  }
+  for (int s = 0; s < 4; ++s) ps.I[s] = (T)I[s];
+  if (!((double)ps.I[0] >= in.min_int && 0 < in.max_scat)) {
+    acc_add(tacc, stride, g, ACC_AREM, (double)ps.I[0]);
+    acc_add(tacc, stride, g, ACC_PHOTONS, 1.0);
+    return false;
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------ sample phase
+// One scattering event of src/gpu.jl:209-291 up to the collection: records the
+// reciprocal-path state, runs the rejection loop (scatter + free path + boundary test),
+// absorbs, and writes the event's collection parameters. The move to the new position
+// is applied here; the escaped-intensity renormalisation waits for the collect phase.
+template <typename T>
+__device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTables<T>& B,
+                            EventP<T>& ev, double* tacc, size_t stride, size_t g,
+                            unsigned* status, bool& dead) {
+  dead = false;
+  const int n = ++ps.n;
+  const DevScatterer& s1 = in.scat[in.layers[0].scat];
+  const Frame<T> inc{(T)in.inc[0], (T)in.inc[1], (T)in.inc[2], (T)in.inc[3]};
+
+  // Incremental forward / backward fields (forward_E, backward_E of src/utils.jl:199-241).
+  if (in.compute_cb) {
+    if (n == 1) {
+      ps.x1[0] = ps.x[0];
+      ps.x1[1] = ps.x[1];
+      ps.x1[2] = ps.x[2];
+      ps.idx1 = ps.idx;
+      double nr = sqrt(in.Ei[0] * in.Ei[0] + in.Ei[1] * in.Ei[1] + in.Ei[2] * in.Ei[2] +
+                       in.Ei[3] * in.Ei[3]);
+      for (int s = 0; s < 4; ++s) ps.A[s] = (T)(in.Ei[s] / nr);
+      ps.logA = log(nr);
+      for (int s = 0; s < 8; ++s) ps.L[s] = T(0);
+      ps.L[0] = T(1);
+      ps.L[6] = T(1);
+      ps.logL = 0.0;
+    } else {
+      if (n == 2) {
+        ps.k2[0] = ps.k[0];
+        ps.k2[1] = ps.k[1];
+        ps.k2[2] = ps.k[2];
+      }
+      Frame<T> fr = n == 2 ? inc : spherical(ps.kprev[0], ps.kprev[1], ps.kprev[2]);
+      T m[8], a[4];
+      update_E_matrix(fr, ps.k[0], ps.k[1], ps.k[2], s1.kind, s1.S, s1.ntheta, m);
+      mat2_vec(m, ps.A, a);
+      T na = MT<T>::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3]);
+      T ina = T(1) / na;
+      for (int s = 0; s < 4; ++s) ps.A[s] = a[s] * ina;
+      ps.logA += log((double)na);
+      if (n >= 3) {
+        Frame<T> fm = spherical(-ps.k[0], -ps.k[1], -ps.k[2]);
+        update_E_matrix(fm, -ps.kprev[0], -ps.kprev[1], -ps.kprev[2], s1.kind, s1.S, s1.ntheta, m);
+        mat2_mul(ps.L, m, ps.L);
+        T nl = T(0);
+        for (int s = 0; s < 8; ++s) nl += ps.L[s] * ps.L[s];
+        nl = MT<T>::sqrt(nl);
+        T inl = T(1) / nl;
+        for (int s = 0; s < 8; ++s) ps.L[s] *= inl;
+        ps.logL += log((double)nl);
+      }
+    }
+    ps.kprev[0] = ps.k[0];
+    ps.kprev[1] = ps.k[1];
+    ps.kprev[2] = ps.k[2];
+  }
+
+  // Rejection loop (src/gpu.jl:215-256).
+  const int idx = ps.idx;
+  const DevLayer& L = in.layers[idx];
+  const DevScatterer& sc = in.scat[L.scat];
+  const Frame<T> ks = spherical(ps.k[0], ps.k[1], ps.k[2]);
+  const T* I = ps.I;
+  T Ip[4], kp[3];
+  double xp[3];
+  int idxp = idx;
+  unsigned a = 0;
+  int kcap = 0;
+  for (;; ++a) {
+    if (a >= MAX_ATTEMPTS) {
+      atomicOr(status, 1u);
+      acc_add(tacc, stride, g, ACC_REJECT_CAP, 1.0);
+      dead = true;
+      return 0;
+    }
+    Draw d = draw(in.key0, in.key1, ps.id, (uint32_t)n, a);
+    T u0 = u01<T>(d.r[0]), u1 = u01<T>(d.r[1]), u2 = u01<T>(d.r[2]);
+    // scatter (src/utils.jl:294-323)
+    T mu = sample_mu<T>(sc.kind, sc.csrn, sc.rp, u0);
+    PMat<T> P = phase_eval<T>(sc.kind, sc.F, sc.ntheta, mu);
+    T den = P.p11 * I[0];
+    T eq = -P.p12 * I[1] / den, eu = -P.p12 * I[2] / den;
+    T ee = MT<T>::sqrt(eq * eq + eu * eu);
+    T phi;
+    if (ee > T(1e-12)) {
+      T gam = MT<T>::acos(clamp1(eq / ee));
+      if (eu < T(0)) gam = (T)(2 * PI_D) - gam;
+      T sg, cg;
+      MT<T>::sincos(gam, &sg, &cg);
+      T ma = (T)(4 * PI_D) * u1 + gam - ee * sg;
+      T ea = kepler<T>(ma, ee, kcap);
+      phi = T(0.5) * (ea - gam);
+    } else {
+      phi = (T)(2 * PI_D) * u1;
+    }
+    T st = MT<T>::sqrt(fmax(T(1) - mu * mu, T(0)));
+    T sphi, cphi;
+    MT<T>::sincos(phi, &sphi, &cphi);
+    T lx = st * cphi, ly = st * sphi, lz = mu;
+    ray_to_norm(ks, lx, ly, lz, kp[0], kp[1], kp[2]);
+    // update_I(sca, I, k', ks) with the ray-frame direction known exactly
+    Frame<T> kls = spherical(lx, ly, lz);
+    T ehx, ehy;
+    basis_h(kp[0], kp[1], ehx, ehy);
+    T cpsi, spsi;
+    psi_angles(ks, kls, ehx, ehy, T(-1), cpsi, spsi);
+    T q = I[1], u = I[2];
+    rotate(kls.cp * kls.cp - kls.sp * kls.sp, T(-2) * kls.sp * kls.cp, q, u);
+    Ip[0] = P.p11 * I[0] + P.p12 * q;
+    Ip[1] = P.p12 * I[0] + P.p11 * q;
+    Ip[2] = P.p33 * u + P.p34 * I[3];
+    Ip[3] = -P.p34 * u + P.p33 * I[3];
+    rotate(cpsi * cpsi - spsi * spsi, T(2) * spsi * cpsi, Ip[1], Ip[2]);
+    // free path and boundary test
+    T t = -MT<T>::log(u2);
+    for (int s = 0; s < 3; ++s) xp[s] = ps.x[s] + (double)t * (double)kp[s];
+    int pb;
+    if (in.geom == 0) {
+      pb = xp[2] > 0 ? -1 : ((!L.inf && xp[2] < -L.tau) ? 1 : 0);
+    } else {
+      double r2 = xp[0] * xp[0] + xp[1] * xp[1] + xp[2] * xp[2];
+      pb = sqrt(r2) > in.layers[0].tau ? -2 : 0;
+    }
+    idxp = idx + pb;
+    if (pb == -2) continue;
+    if (pb == -1) {
+      if (idxp < 0) continue;
+      xp[0] = ps.x[0];
+      xp[1] = ps.x[1];
+      xp[2] = -L.tau;
+      break;
+    }
+    if (pb == 1) {
+      if (idxp > in.n_layers - 1) continue;
+      xp[0] = ps.x[0];
+      xp[1] = ps.x[1];
+      xp[2] = 0.0;
+      break;
+    }
+    break;
+  }
+  if (kcap) {
+    atomicOr(status, 2u);
+    acc_add(tacc, stride, g, ACC_KEPLER_CAP, 1.0);
+  }
+
+  // Absorption (src/gpu.jl:259-260)
+  T Ia[4];
+  const T om = (T)L.omega;
+  acc_add(tacc, stride, g, ACC_AABS, (1.0 - L.omega) * (double)I[0]);
+  for (int s = 0; s < 4; ++s) Ia[s] = I[s] * om;
+
+  // Proximity tests (src/gpu.jl:266-267)
+  double mdf, mdl;
+  if (in.geom == 0) {
+    mdf = idx == 0 ? fabs(ps.x[2]) : INFINITY;
+    mdl = (idx == in.n_layers - 1 && !L.inf) ? L.tau - fabs(ps.x[2]) : INFINITY;
+  } else {
+    mdf = in.layers[0].tau -
+          sqrt(ps.x[0] * ps.x[0] + ps.x[1] * ps.x[1] + ps.x[2] * ps.x[2]);
+    mdl = INFINITY;
+  }
+  const bool up = mdf <= in.tau0, dn = mdl <= in.tau0;
+  const bool cb = in.compute_cb && (up || dn);
+  int flags = (up ? EV_UP : 0) | (dn ? EV_DN : 0) | (cb ? EV_CB : 0) | ((cb && n > 1) ? EV_CBN : 0);
+
+  // Event parameters shared by RT and CB.
+  for (int s = 0; s < 4; ++s) ev.I[s] = Ia[s];
+  ev.fct = ks.ct;
+  ev.fst = ks.st;
+  ev.fcp = ks.cp;
+  ev.fsp = ks.sp;
+  if (in.geom == 0) {
+    ev.a_up = (T)(-ps.x[2]);
+    ev.a_dn = L.inf ? (T)INFINITY : (T)(ps.x[2] + L.tau);
+  } else {
+    double tau = in.layers[0].tau;
+    ev.xax = (T)ps.x[0];
+    ev.xay = (T)ps.x[1];
+    ev.xaz = (T)ps.x[2];
+    double D = tau * tau - (ps.x[0] * ps.x[0] + ps.x[1] * ps.x[1] + ps.x[2] * ps.x[2]);
+    ev.Da = (T)(D > 0 ? D : 0);
+  }
+  ev.flags = flags;
+  ev.layer = L.scat;
+
+  if (cb && n > 1) {
+    // Reciprocal-path setup of collect_cb_gpu! (src/gpu.jl:55-88).
+    const Frame<T> kbs = spherical(-ps.k2[0], -ps.k2[1], -ps.k2[2]);
+    ev.bct = kbs.ct;
+    ev.bst = kbs.st;
+    ev.bcp = kbs.cp;
+    ev.bsp = kbs.sp;
+    T m[8], Ei[4], tmp[4], b[4];
+    for (int s = 0; s < 4; ++s) Ei[s] = (T)in.Ei[s];
+    update_E_matrix(inc, -ps.k[0], -ps.k[1], -ps.k[2], s1.kind, s1.S, s1.ntheta, m);
+    mat2_vec(m, Ei, tmp);
+    mat2_vec(ps.L, tmp, b);
+    const T kf0x = (T)in.kf0[0], kf0y = (T)in.kf0[1], kf0z = (T)in.kf0[2];
+    const T eh0x = (T)in.eh0[0], eh0y = (T)in.eh0[1];
+    T Iaf0[4];
+    update_I(ks, Ia, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.F, s1.ntheta, Iaf0);
+    T Ef[4] = {ps.A[0], ps.A[1], ps.A[2], ps.A[3]};
+    update_E(ks, Ef, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.S, s1.ntheta);
+    T nf = Ef[0] * Ef[0] + Ef[1] * Ef[1] + Ef[2] * Ef[2] + Ef[3] * Ef[3];
+    T c = MT<T>::sqrt(Iaf0[0] / nf);
+    T rb = (T)exp(ps.logL - ps.logA) * c;
+    for (int s = 0; s < 4; ++s) {
+      ev.ea[s] = ps.A[s] * c;
+      ev.eb[s] = b[s] * rb;
+    }
+    double ta0 = dist_d(in, ps.x, in.kf0[0], in.kf0[1], in.kf0[2], idx);
+    double tb0 = dist_d(in, ps.x1, in.kf0[0], in.kf0[1], in.kf0[2], ps.idx1);
+    ev.tab2 = (T)((ta0 - tb0) * LOG2E_D);
+    double dx = in.kl1 * (ps.x[0] - ps.x1[0]) / (2 * PI_D);
+    double dy = in.kl1 * (ps.x[1] - ps.x1[1]) / (2 * PI_D);
+    double dz = in.kl1 * (ps.x[2] - ps.x1[2]) / (2 * PI_D);
+    ev.v1 = (T)(in.Rkfs[0] * dx + in.Rkfs[1] * dy + in.Rkfs[2] * dz);
+    ev.v2 = (T)(in.Rkfs[3] * dx + in.Rkfs[4] * dy + in.Rkfs[5] * dz);
+    ev.v3 = (T)(in.Rkfs[6] * dx + in.Rkfs[7] * dy + in.Rkfs[8] * dz);
+    if (in.geom == 0) {
+      const DevLayer& L1 = in.layers[ps.idx1];
+      ev.b_up = (T)(-ps.x1[2]);
+      ev.b_dn = L1.inf ? (T)INFINITY : (T)(ps.x1[2] + L1.tau);
+    } else {
+      double tau = in.layers[0].tau;
+      ev.xbx = (T)ps.x1[0];
+      ev.xby = (T)ps.x1[1];
+      ev.xbz = (T)ps.x1[2];
+      double D = tau * tau - (ps.x1[0] * ps.x1[0] + ps.x1[1] * ps.x1[1] + ps.x1[2] * ps.x1[2]);
+      ev.Db = (T)(D > 0 ? D : 0);
+    }
+  }
+
+  // Counters and the pending state change (applied now; the weight waits).
+  double evals_rt = (double)B.nphi * ((up ? (B.up1 - B.up0) : 0) + (dn ? (B.lo1 - B.lo0) : 0));
+  acc_add(tacc, stride, g, ACC_EVENTS, 1.0);
+  acc_add(tacc, stride, g, ACC_ATTEMPTS, (double)(a + 1));
+  acc_add(tacc, stride, g, ACC_RT, evals_rt);
+  if (cb) acc_add(tacc, stride, g, n > 1 ? ACC_CBN : ACC_CB1, (double)B.nthetab * B.nphib);
+
+  T inv = T(1) / Ip[0];
+  ps.Ih[0] = T(1);
+  ps.Ih[1] = Ip[1] * inv;
+  ps.Ih[2] = Ip[2] * inv;
+  ps.Ih[3] = Ip[3] * inv;
+  ps.wI = Ia[0];
+  for (int s = 0; s < 3; ++s) {
+    ps.k[s] = kp[s];
+    ps.x[s] = xp[s];
+  }
+  ps.idx = idxp;
+  return flags;
+}
+
+// ------------------------------------------------------------------ collect: RT tile
+template <typename T, int NB>
+struct RTLane {
+  T st[NB], ct[NB], g[NB], w[NB];
+  T cb, sb;
+  T acc[NB][4];
+};
+
+template <typename T, int NB, bool MIE, bool SPHERE>
+__device__ __forceinline__ T rt_event(RTLane<T, NB>& R, const EventP<T>& E, const float4* F,
+                                      int ntheta, T tau0l, bool upper) {
+  const T fct = E.fct, fst = E.fst, fcp = E.fcp, fsp = E.fsp;
+  const T sD = R.sb * fcp - R.cb * fsp, cD = R.cb * fcp + R.sb * fsp;
+  const T a1 = fct * cD, a3 = fst * cD, bq = fct * sD, c4 = fst * sD;
+  const T I0 = E.I[0], I1 = E.I[1], I2 = E.I[2], I3 = E.I[3];
+  T a = upper ? E.a_up : E.a_dn;
+  T qx = T(0), xz = T(0), D = T(0);
+  if (SPHERE) {
+    qx = R.cb * E.xax + R.sb * E.xay;
+    xz = E.xaz;
+    D = E.Da;
+  }
+  T esc = T(0);
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    const T k1 = R.st[i] * a1 - R.ct[i] * fst;
+    const T k2 = R.st[i] * sD;
+    const T k3 = R.st[i] * a3 + R.ct[i] * fct;
+    const T s2 = k1 * k1 + k2 * k2;
+    T cpk, spk, stk, ctk;
+    if (s2 < T(1e-24)) {
+      cpk = T(1);
+      spk = T(0);
+      stk = T(0);
+      ctk = k3 > T(0) ? T(1) : (k3 < T(0) ? T(-1) : T(0));
+    } else {
+      const T r = MT<T>::rsqrt(s2);
+      cpk = k1 * r;
+      spk = k2 * r;
+      stk = s2 * r;
+      ctk = k3;
+    }
+    const T c2 = cpk * cpk - spk * spk, sr = T(-2) * spk * cpk;
+    const T q = c2 * I1 + sr * I2, u = -sr * I1 + c2 * I2;
+    const T cpsi = spk * bq + cpk * cD;
+    const T spsi = ctk * (spk * cD - cpk * bq) + stk * c4;
+    const T c2p = cpsi * cpsi - spsi * spsi, s2p = T(2) * spsi * cpsi;
+    PMat<T> P;
+    if (MIE) {
+      P = phase_eval<T>(1, F, ntheta, k3);
+    } else {
+      const T m2 = k3 * k3;
+      P = PMat<T>{T(0.75) + T(0.75) * m2, T(-0.75) + T(0.75) * m2, T(1.5) * k3, T(0)};
+    }
+    const T o0 = P.p11 * I0 + P.p12 * q;
+    const T o1 = P.p12 * I0 + P.p11 * q;
+    const T o2 = P.p33 * u + P.p34 * I3;
+    const T o3 = -P.p34 * u + P.p33 * I3;
+    const T r1 = c2p * o1 + s2p * o2, r2 = -s2p * o1 + c2p * o2;
+    T t2;
+    if (SPHERE) {
+      const T kx = R.st[i] * qx + R.ct[i] * xz;
+      t2 = sphere_t(kx, D) * T(LOG2E_D);
+    } else {
+      t2 = a * R.g[i];
+    }
+    const T wgt = t2 <= tau0l ? MT<T>::exp2n(t2) * R.w[i] : T(0);
+    R.acc[i][0] += o0 * wgt;
+    R.acc[i][1] += r1 * wgt;
+    R.acc[i][2] += r2 * wgt;
+    R.acc[i][3] += o3 * wgt;
+    esc += o0 * wgt;
+  }
+  return esc;
+}
+
+template <typename T, int NB, int BS>
+__device__ void rt_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool upper, int pc) {
+  const int lane = threadIdx.x & 31;
+  const int r0 = upper ? B.up0 : B.lo0, r1 = upper ? B.up1 : B.lo1;
+  const int ngrp = (r1 - r0 + NB - 1) / NB;
+  const int item = tile * 32 + lane;
+  const bool lane_ok = item < ngrp * B.nphi;
+  const int it = lane_ok ? item : 0;
+  const int j2 = it % B.nphi, grp = it / B.nphi;
+  RTLane<T, NB> R;
+  R.cb = B.cp[j2];
+  R.sb = B.sp[j2];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    int j1 = r0 + grp * NB + i;
+    bool ok = lane_ok && j1 < r1;
+    int jj = ok ? j1 : r0;
+    R.st[i] = B.st[jj];
+    R.ct[i] = B.ct[jj];
+    R.g[i] = B.g[jj];
+    R.w[i] = ok ? B.w[jj] : T(0);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) R.acc[i][s] = T(0);
+  }
+  const DevInstance& in = sh.inst;
+  const T tau0l = (T)(in.tau0 * LOG2E_D);
+  const int li = upper ? 0 : 1;
+  const int ne = sh.cnt[pc][li];
+  T* escarr = upper ? sh.esc_up : sh.esc_dn;
+  const bool sphere = in.geom == 1;
+  for (int q = 0; q < ne; ++q) {
+    const int e = sh.list[li][q];
+    const EventP<T>& E = sh.ev[e];
+    const DevScatterer& sc = in.scat[E.layer];
+    T esc;
+    if (sc.kind == 1) {
+      esc = sphere ? rt_event<T, NB, true, true>(R, E, sc.F, sc.ntheta, tau0l, upper)
+                   : rt_event<T, NB, true, false>(R, E, sc.F, sc.ntheta, tau0l, upper);
+    } else {
+      esc = sphere ? rt_event<T, NB, false, true>(R, E, sc.F, sc.ntheta, tau0l, upper)
+                   : rt_event<T, NB, false, false>(R, E, sc.F, sc.ntheta, tau0l, upper);
+    }
+    esc = warp_sum(esc);
+    if (lane == 0) atomicAdd(&escarr[e], esc);
+  }
+  if (lane_ok) {
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      int j1 = r0 + grp * NB + i;
+      if (j1 < r1) {
+        double* dst = in.Irt + 4 * ((size_t)j2 * B.ntheta + j1);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) atomicAdd(dst + s, (double)R.acc[i][s]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ collect: CB tile
+template <typename T, int NB>
+struct CBLane {
+  T kx[NB], ky[NB], kz[NB], ehx[NB], ehy[NB], g[NB], cf[NB], sf[NB], c1[NB], c2[NB], c3[NB];
+  bool upb[NB];
+  T acc[NB][4];
+  T lad[NB];
+};
+
+template <typename T, int NB, bool MIE, bool SPHERE>
+__device__ __forceinline__ T cbn_event(CBLane<T, NB>& C, const EventP<T>& E, const DevScatterer& s1,
+                                       T tau0l, bool peak_lane) {
+  const Frame<T> fa{E.fct, E.fst, E.fcp, E.fsp};
+  const Frame<T> fb{E.bct, E.bst, E.bcp, E.bsp};
+  T pk = T(0);
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    T ea[4] = {E.ea[0], E.ea[1], E.ea[2], E.ea[3]};
+    T eb[4] = {E.eb[0], E.eb[1], E.eb[2], E.eb[3]};
+    update_E<T>(fa, ea, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.S, s1.ntheta);
+    update_E<T>(fb, eb, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.S, s1.ntheta);
+    // Phase kl (ki + kf).(xa - xb) in turns, cancellation-free in the backscatter frame.
+    const T turns = C.c1[i] * E.v1 + C.c2[i] * E.v2 + C.c3[i] * E.v3;
+    const T fr = turns - MT<T>::rint(turns);
+    T sn, cs;
+    MT<T>::sincospi(T(2) * fr, &sn, &cs);
+    T ta2, tb2;
+    if (SPHERE) {
+      ta2 = sphere_t(C.kx[i] * E.xax + C.ky[i] * E.xay + C.kz[i] * E.xaz, E.Da) * T(LOG2E_D);
+      tb2 = sphere_t(C.kx[i] * E.xbx + C.ky[i] * E.xby + C.kz[i] * E.xbz, E.Db) * T(LOG2E_D);
+    } else {
+      ta2 = (C.upb[i] ? E.a_up : E.a_dn) * C.g[i];
+      tb2 = (C.upb[i] ? E.b_up : E.b_dn) * C.g[i];
+    }
+    tb2 += E.tab2;
+    const bool ma = ta2 <= tau0l;
+    const T na = MT<T>::exp2n(T(0.5) * ta2);
+    const T nb = MT<T>::fabs(tb2) <= tau0l ? MT<T>::exp2n(T(0.5) * tb2) : T(0);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      ea[s] *= na;
+      eb[s] *= nb;
+    }
+    const T Ia = ea[0] * ea[0] + ea[1] * ea[1] + ea[2] * ea[2] + ea[3] * ea[3];
+    const T Ib = eb[0] * eb[0] + eb[1] * eb[1] + eb[2] * eb[2] + eb[3] * eb[3];
+    const T c1r = ea[0] * cs - ea[1] * sn + eb[0], c1i = ea[0] * sn + ea[1] * cs + eb[1];
+    const T c2r = ea[2] * cs - ea[3] * sn + eb[2], c2i = ea[2] * sn + ea[3] * cs + eb[3];
+    const T qh = c1r * c1r + c1i * c1i, qv = c2r * c2r + c2i * c2i;
+    T S0 = qh + qv, S1 = qv - qh;
+    T S2 = T(2) * (c2r * c1r + c2i * c1i), S3 = T(-2) * (c2i * c1r - c2r * c1i);
+    const T den = Ia + Ib;
+    const bool ok = ma && den > T(0);
+    const T scl = ok ? Ia / den : T(0);
+    S0 *= scl;
+    S1 *= scl;
+    S2 *= scl;
+    S3 *= scl;
+    rotate(C.cf[i], C.sf[i], S1, S2);
+    C.acc[i][0] += ok ? S0 : T(0);
+    C.acc[i][1] += ok ? S1 : T(0);
+    C.acc[i][2] += ok ? S2 : T(0);
+    C.acc[i][3] += ok ? S3 : T(0);
+    C.lad[i] += ok ? Ia : T(0);
+    if (i == 0 && peak_lane) pk = ok ? S0 : T(0);
+  }
+  return pk;
+}
+
+template <typename T, int NB, bool MIE, bool SPHERE>
+__device__ __forceinline__ T cb1_event(CBLane<T, NB>& C, const EventP<T>& E, const DevScatterer& s1,
+                                       T tau0l, bool peak_lane) {
+  const Frame<T> fa{E.fct, E.fst, E.fcp, E.fsp};
+  T pk = T(0);
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    T o[4];
+    update_I<T>(fa, E.I, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.F, s1.ntheta,
+                o);
+    T ta2;
+    if (SPHERE)
+      ta2 = sphere_t(C.kx[i] * E.xax + C.ky[i] * E.xay + C.kz[i] * E.xaz, E.Da) * T(LOG2E_D);
+    else
+      ta2 = (C.upb[i] ? E.a_up : E.a_dn) * C.g[i];
+    const bool ma = ta2 <= tau0l;
+    const T w = ma ? MT<T>::exp2n(ta2) : T(0);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) o[s] *= w;
+    rotate(C.cf[i], C.sf[i], o[1], o[2]);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) C.acc[i][s] += ma ? o[s] : T(0);
+    C.lad[i] += ma ? o[0] : T(0);
+    if (i == 0 && peak_lane) pk = ma ? o[0] : T(0);
+  }
+  return pk;
+}
+
+template <typename T, int NB, int BS>
+__device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int pc) {
+  const int lane = threadIdx.x & 31;
+  const int ngrp = (B.nthetab + NB - 1) / NB;
+  const int item = tile * 32 + lane;
+  const bool lane_ok = item < ngrp * B.nphib;
+  const int it = lane_ok ? item : 0;
+  const int j2 = it % B.nphib, grp = it / B.nphib;
+  CBLane<T, NB> C;
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    int j1 = grp * NB + i;
+    bool ok = lane_ok && j1 < B.nthetab;
+    int b = ok ? j2 * B.nthetab + j1 : 0;
+    C.kx[i] = B.kfx[b];
+    C.ky[i] = B.kfy[b];
+    C.kz[i] = B.kfz[b];
+    C.ehx[i] = B.ehx[b];
+    C.ehy[i] = B.ehy[b];
+    C.g[i] = B.gb[b];
+    C.cf[i] = B.cf2[b];
+    C.sf[i] = B.sf2[b];
+    C.c1[i] = B.c1[b];
+    C.c2[i] = B.c2[b];
+    C.c3[i] = B.c3[b];
+    C.upb[i] = B.upb[b] != 0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) C.acc[i][s] = T(0);
+    C.lad[i] = T(0);
+  }
+  const bool peak_lane = lane_ok && j2 == 0 && grp == 0;
+  const DevInstance& in = sh.inst;
+  const DevScatterer& s1 = in.scat[in.layers[0].scat];
+  const T tau0l = (T)(in.tau0 * LOG2E_D);
+  const bool sphere = in.geom == 1, mie = s1.kind == 1;
+  const int nn = sh.cnt[pc][2];
+  for (int q = 0; q < nn; ++q) {
+    const int e = sh.list[2][q];
+    const EventP<T>& E = sh.ev[e];
+    T pk;
+    if (mie)
+      pk = sphere ? cbn_event<T, NB, true, true>(C, E, s1, tau0l, peak_lane)
+                  : cbn_event<T, NB, true, false>(C, E, s1, tau0l, peak_lane);
+    else
+      pk = sphere ? cbn_event<T, NB, false, true>(C, E, s1, tau0l, peak_lane)
+                  : cbn_event<T, NB, false, false>(C, E, s1, tau0l, peak_lane);
+    if (peak_lane) sh.peak[e] = pk;
+  }
+  const int n1 = sh.cnt[pc][3];
+  for (int q = 0; q < n1; ++q) {
+    const int e = sh.list[3][q];
+    const EventP<T>& E = sh.ev[e];
+    T pk;
+    if (mie)
+      pk = sphere ? cb1_event<T, NB, true, true>(C, E, s1, tau0l, peak_lane)
+                  : cb1_event<T, NB, true, false>(C, E, s1, tau0l, peak_lane);
+    else
+      pk = sphere ? cb1_event<T, NB, false, true>(C, E, s1, tau0l, peak_lane)
+                  : cb1_event<T, NB, false, false>(C, E, s1, tau0l, peak_lane);
+    if (peak_lane) sh.peak[e] = pk;
+  }
+  if (lane_ok) {
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      int j1 = grp * NB + i;
+      if (j1 < B.nthetab) {
+        size_t b = (size_t)j2 * B.nthetab + j1;
+        double* dst = in.Icb + 4 * b;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) atomicAdd(dst + s, (double)C.acc[i][s]);
+        atomicAdd(in.ladder + b, (double)C.lad[i]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ the kernel
+template <typename T, int BS, int NBR, int NBC, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  Shared<T, BS>& sh = *reinterpret_cast<Shared<T, BS>*>(smraw);
+  float4* tables = reinterpret_cast<float4*>(smraw + sizeof(Shared<T, BS>));
+  const int tid = threadIdx.x, lane = tid & 31;
+  const size_t g = (size_t)blockIdx.x * BS + tid;
+  const size_t stride = (size_t)gridDim.x * BS;
+
+  if (tid == 0) {
+    sh.cur = next_instance(p, -1);
+    sh.exhausted = 0;
+    sh.item_next = 0;
+    for (int i = 0; i < 8; ++i) (&sh.cnt[0][0])[i] = 0;
+  }
+  for (int k = 0; k < NACC; ++k) p.tacc[(size_t)k * stride + g] = 0.0;
+  __syncthreads();
+  if (sh.cur < 0) return;
+  stage_instance<T, BS>(sh, tables, p, sh.cur);
+
+  bool alive = false;
+  int pc = 0;
+  PState<T> ps;
+  for (;;) {
+    const DevInstance& in = sh.inst;
+    const BinTables<T>& B = *reinterpret_cast<const BinTables<T>*>(in.bins);
+    // ---- claim new photons (warp-aggregated) and start them
+    {
+      const bool want_b = !alive && !sh.exhausted;
+      const unsigned want = __ballot_sync(0xffffffffu, want_b);
+      if (want) {
+        const int leader = __ffs(want) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(in.claim, (unsigned long long)__popc(want));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (want_b) {
+          unsigned long long my = base + __popc(want & ((1u << lane) - 1u));
+          if ((long long)my < in.n_photons) {
+            alive = start_photon<T>(ps, in, (unsigned long long)in.photon_begin + my, p.tacc, stride,
+                                    g, p.status);
+          } else {
+            sh.exhausted = 1;
+          }
+        }
+      }
+    }
+    // ---- sample phase
+    int flags = 0;
+    if (alive) {
+      bool dead = false;
+      flags = sample_event<T>(ps, in, B, sh.ev[tid], p.tacc, stride, g, p.status, dead);
+      if (dead) {
+        alive = false;
+        flags = 0;
+      }
+      sh.esc_up[tid] = T(0);
+      sh.esc_dn[tid] = T(0);
+      sh.peak[tid] = T(0);
+      if (alive) ps_store(ps, p.state, stride, g);
+    }
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      const int bit = l == 0 ? EV_UP : (l == 1 ? EV_DN : (l == 2 ? EV_CBN : EV_CB));
+      bool in_list = (flags & bit) != 0;
+      if (l == 3) in_list = in_list && !(flags & EV_CBN);
+      const unsigned m = __ballot_sync(0xffffffffu, in_list);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&sh.cnt[pc][l], __popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (in_list) sh.list[l][base + __popc(m & ((1u << lane) - 1u))] = (unsigned short)tid;
+      }
+    }
+    const int nalive = __syncthreads_count(alive);
+    if (nalive == 0) {
+      if (!sh.exhausted) continue;
+      // This block has finished its part of the instance: fold the per-thread
+      // accumulators into the instance's totals and move on.
+      for (int k = 0; k < NACC; ++k) {
+        double v = p.tacc[(size_t)k * stride + g];
+        p.tacc[(size_t)k * stride + g] = 0.0;
+        v = warp_sum(v);
+        if (lane == 0 && v != 0.0) atomicAdd(in.acc + k, v);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        sh.cur = next_instance(p, sh.cur);
+        sh.exhausted = 0;
+        for (int i = 0; i < 8; ++i) (&sh.cnt[0][0])[i] = 0;
+      }
+      __syncthreads();
+      if (sh.cur < 0) break;
+      stage_instance<T, BS>(sh, tables, p, sh.cur);
+      continue;
+    }
+    // ---- collect phase
+    {
+      const int nu = sh.cnt[pc][0], nd = sh.cnt[pc][1], nc = sh.cnt[pc][2] + sh.cnt[pc][3];
+      const int tcb = nc ? (B.nphib * ((B.nthetab + NBC - 1) / NBC) + 31) / 32 : 0;
+      const int tup = nu ? (B.nphi * ((B.up1 - B.up0 + NBR - 1) / NBR) + 31) / 32 : 0;
+      const int tdn = nd ? (B.nphi * ((B.lo1 - B.lo0 + NBR - 1) / NBR) + 31) / 32 : 0;
+      const int total = tcb + tup + tdn;
+      if (tid == 0)
+        for (int l = 0; l < 4; ++l) sh.cnt[pc ^ 1][l] = 0;
+      for (;;) {
+        int w = 0;
+        if (lane == 0) w = atomicAdd(&sh.item_next, 1);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= total) break;
+        if (w < tcb)
+          cb_tile<T, NBC, BS>(sh, B, w, pc);
+        else if (w < tcb + tup)
+          rt_tile<T, NBR, BS>(sh, B, w - tcb, true, pc);
+        else
+          rt_tile<T, NBR, BS>(sh, B, w - tcb - tup, false, pc);
+      }
+    }
+    __syncthreads();
+    // ---- finish phase: renormalise by the escaped intensity (src/gpu.jl:285-294)
+    if (tid == 0) sh.item_next = 0;
+    if (alive) {
+      ps_load(ps, p.state, stride, g);
+      const double eu = (double)sh.esc_up[tid], ed = (double)sh.esc_dn[tid];
+      acc_add(p.tacc, stride, g, ACC_AREF, eu);
+      acc_add(p.tacc, stride, g, ACC_ATRANS, ed);
+      ps.peak += (double)sh.peak[tid];
+      const T wnew = ps.wI - (T)(eu + ed);
+      for (int s = 0; s < 4; ++s) ps.I[s] = ps.Ih[s] * wnew;
+      const double i0 = (double)ps.I[0];
+      if (!isfinite(i0)) {
+        atomicOr(p.status, 4u);
+        acc_add(p.tacc, stride, g, ACC_NONFINITE, 1.0);
+        acc_add(p.tacc, stride, g, ACC_PHOTONS, 1.0);
+        alive = false;
+      } else if (!(i0 >= in.min_int && ps.n < in.max_scat)) {
+        acc_add(p.tacc, stride, g, ACC_AREM, i0);
+        acc_add(p.tacc, stride, g, ACC_PEAK, ps.peak);
+        acc_add(p.tacc, stride, g, ACC_PEAK2, ps.peak * ps.peak);
+        acc_add(p.tacc, stride, g, ACC_PHOTONS, 1.0);
+        alive = false;
+      }
+    }
+    pc ^= 1;
+  }
+}
+
+}  // namespace mcrt

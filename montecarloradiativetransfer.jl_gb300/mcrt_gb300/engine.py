@@ -1,0 +1,343 @@
+"""simulate / run_rt on the GPU through libmcrt, mirroring the reference's driver
+(src/MonteCarloRadiativeTransfer.jl:26-291).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, lib
+
+_PREC = {"fp32": _lib.FP32, "fp64": _lib.FP64}
+_KERN = {"persistent": _lib.KERNEL_PERSISTENT, "plain": _lib.KERNEL_PLAIN}
+
+
+class Context:
+    """One CUDA device: the library context plus uploaded scatterers (by identity)."""
+
+    def __init__(self, device: int = 0):
+        L = lib()
+        if L.mcrt_device_count() <= 0:
+            raise _lib.MCRTError(_lib.MCRT_ENODEV, "no CUDA device is visible")
+        h = C.c_void_p()
+        check(L.mcrt_ctx_create(int(device), C.byref(h)))
+        self.h = h
+        self.device = device
+        self._scat: Dict[int, Tuple[object, C.c_void_p]] = {}
+
+    def scatterer(self, s) -> C.c_void_p:
+        key = id(s)
+        hit = self._scat.get(key)
+        if hit is not None and hit[0] is s:
+            return hit[1]
+        d = _lib.ScattererDesc()
+        d.kind, d.omega, d.kl = s.kind, s.omega, s.kl
+        keep = []
+        if s.kind == _lib.MIE:
+            F = [np.ascontiguousarray(a, float) for a in (s.F11, s.F12, s.F33, s.F34)]
+            S = [np.ascontiguousarray(np.column_stack([z.real, z.imag]).ravel()) for z in (s.S11, s.S22)]
+            cs = np.ascontiguousarray(s.csrn, float)
+            keep = F + S + [cs]
+            d.n_theta = len(F[0])
+            d.F11, d.F12, d.F33, d.F34 = (dptr(a) for a in F)
+            d.S11, d.S22 = dptr(S[0]), dptr(S[1])
+            d.random_points = len(cs) - 1
+            d.csrn = dptr(cs)
+        h = C.c_void_p()
+        check(lib().mcrt_scatterer_create(self.h, C.byref(d), C.byref(h)))
+        del keep
+        self._scat[key] = (s, h)
+        return h
+
+    def geometry_c(self, g):
+        """C view of a geometry; returns (GeometryC, keep-alive list)."""
+        if g.kind == _lib.PLANE:
+            layers = (_lib.LayerC * len(g.layers))()
+            for i, l in enumerate(g.layers):
+                layers[i] = _lib.LayerC(l.tau, l.omega, int(l.infinite), self.scatterer(l.scatterer))
+            gc = _lib.GeometryC(_lib.PLANE, g.theta, g.phi, len(g.layers), layers)
+        else:
+            layers = (_lib.LayerC * 1)()
+            layers[0] = _lib.LayerC(g.tau, g.omega, 0, self.scatterer(g.scatterer))
+            gc = _lib.GeometryC(_lib.SPHERE, math.pi, 0.0, 1, layers)
+        return gc, [layers]
+
+    def fp32_peak_tflops(self) -> float:
+        v = np.zeros(1)
+        check(lib().mcrt_measure_fp32_peak(self.h, dptr(v)))
+        return float(v[0])
+
+    def close(self) -> None:
+        if self.h:
+            L = lib()
+            for _, h in self._scat.values():
+                L.mcrt_scatterer_destroy(h)
+            self._scat.clear()
+            L.mcrt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default
+
+
+def run_opts(precision="fp32", kernel="persistent", seed=1, instance=0, rng_mode=0, photon_begin=0,
+             block_size=0, blocks_per_sm=0, plain_threads=0) -> _lib.RunOpts:
+    return _lib.RunOpts(_PREC[precision], _KERN[kernel], int(seed), int(instance), int(rng_mode),
+                        int(photon_begin), int(block_size), int(blocks_per_sm), int(plain_threads))
+
+
+def _views(cfg, Irt, Icb, lad):
+    """Reference layouts: Irt[s, j1, j2] of shape (4, Ntheta, Nphi), Icb (4, Ntheta_b, Nphi_b)."""
+    irt = Irt.reshape(cfg.Nphi, cfg.Ntheta, 4).transpose(2, 1, 0)
+    icb = Icb.reshape(cfg.Nphib, cfg.Nthetab, 4).transpose(2, 1, 0)
+    ld = lad.reshape(cfg.Nphib, cfg.Nthetab).T
+    return irt, icb, ld
+
+
+def simulate(cfg, g, I0, *, use_gpu: bool = True, ctx: Optional[Context] = None, with_extras: bool = False,
+             **opts):
+    """simulate(cfg, g, I0; use_gpu) of src/MonteCarloRadiativeTransfer.jl:26-85.
+
+    Returns ``(Adt, Aabs, Aref, Atrans, Arem, Irt, Icb)`` divided by ``number_of_rays``,
+    with ``Irt`` of shape (4, Ntheta, Nphi) and ``Icb`` of shape (4, Ntheta_b, Nphi_b).
+    ``opts`` are the launch options of :func:`run_opts` (precision, kernel, seed,
+    instance, rng_mode, ...). With ``with_extras`` an eighth element is a dict holding
+    the incoherent CB tally ``ladder`` and the launch ``stats``.
+    """
+    if not use_gpu:
+        raise NotImplementedError(
+            "this package runs the transport on the GPU only; the CPU path is the reference's")
+    ctx = ctx or default_context()
+    g.validate()
+    cc = cfg.to_c()
+    gc, keep = ctx.geometry_c(g)
+    I = np.ascontiguousarray(I0, float)
+    A = np.zeros(5)
+    Irt = np.zeros(4 * cfg.Ntheta * cfg.Nphi)
+    Icb = np.zeros(4 * cfg.Nthetab * cfg.Nphib)
+    lad = np.zeros(cfg.Nthetab * cfg.Nphib)
+    st = _lib.Stats()
+    o = run_opts(**opts)
+    check(lib().mcrt_simulate(ctx.h, C.byref(cc), C.byref(gc), dptr(I), C.byref(o), dptr(A),
+                              dptr(Irt), dptr(Icb), dptr(lad), C.byref(st)))
+    irt, icb, ld = _views(cfg, Irt, Icb, lad)
+    out = (A[0], A[1], A[2], A[3], A[4], irt, icb)
+    if with_extras:
+        return out + ({"ladder": ld, "stats": st.as_dict()},)
+    return out
+
+
+class Solve:
+    """A resident solve: inputs and tallies stay on the device between launches."""
+
+    def __init__(self, cfg, g, I0, *, ctx: Optional[Context] = None, **opts):
+        self.ctx = ctx or default_context()
+        g.validate()
+        self.cfg = cfg
+        self._cc = cfg.to_c()
+        self._gc, self._keep = self.ctx.geometry_c(g)
+        self._I = np.ascontiguousarray(I0, float)
+        self._o = run_opts(**opts)
+        h = C.c_void_p()
+        check(lib().mcrt_solve_create(self.ctx.h, C.byref(self._cc), C.byref(self._gc), dptr(self._I),
+                                      C.byref(self._o), C.byref(h)))
+        self.h = h
+        n = cfg
+        self.A = np.zeros(5)
+        self.Irt = np.zeros(4 * n.Ntheta * n.Nphi)
+        self.Icb = np.zeros(4 * n.Nthetab * n.Nphib)
+        self.lad = np.zeros(n.Nthetab * n.Nphib)
+        self.stats = _lib.Stats()
+
+    def launch(self, photon_begin: int, n_photons: int) -> None:
+        check(lib().mcrt_solve_launch(self.h, int(photon_begin), int(n_photons)))
+
+    def read(self) -> dict:
+        """Raw (undivided) sums of the last launch."""
+        check(lib().mcrt_solve_read(self.h, dptr(self.A), dptr(self.Irt), dptr(self.Icb), dptr(self.lad),
+                                    C.byref(self.stats)))
+        irt, icb, ld = _views(self.cfg, self.Irt, self.Icb, self.lad)
+        return {"A": self.A.copy(), "Irt": irt.copy(), "Icb": icb.copy(), "ladder": ld.copy(),
+                "stats": self.stats.as_dict()}
+
+    def close(self) -> None:
+        if self.h:
+            lib().mcrt_solve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many simulate() instances in one persistent launch (per-instance work queues).
+
+    ``instances`` is a list of dicts with keys geometry, I0, n_photons, seed, instance.
+    """
+
+    def __init__(self, cfg, instances: Sequence[dict], *, ctx: Optional[Context] = None, **opts):
+        self.ctx = ctx or default_context()
+        self.cfg = cfg
+        self._cc = cfg.to_c()
+        n = len(instances)
+        self._keep = []
+        arr = (_lib.InstanceC * n)()
+        self._gcs = []
+        for i, d in enumerate(instances):
+            d["geometry"].validate()
+            gc, keep = self.ctx.geometry_c(d["geometry"])
+            self._gcs.append(gc)
+            self._keep.append(keep)
+            arr[i].geometry = C.pointer(gc)
+            for s in range(4):
+                arr[i].I0[s] = float(d["I0"][s])
+            arr[i].seed = int(d.get("seed", 1))
+            arr[i].instance = int(d.get("instance", i))
+            arr[i].n_photons = int(d["n_photons"])
+        self._arr = arr
+        self._o = run_opts(**opts)
+        h = C.c_void_p()
+        check(lib().mcrt_batch_create(self.ctx.h, C.byref(self._cc), arr, n, C.byref(self._o), C.byref(h)))
+        self.h = h
+        self.n = n
+
+    def launch(self) -> None:
+        check(lib().mcrt_batch_launch(self.h))
+
+    def read(self, i: int) -> dict:
+        cfg = self.cfg
+        A = np.zeros(5)
+        Irt = np.zeros(4 * cfg.Ntheta * cfg.Nphi)
+        Icb = np.zeros(4 * cfg.Nthetab * cfg.Nphib)
+        lad = np.zeros(cfg.Nthetab * cfg.Nphib)
+        st = _lib.Stats()
+        check(lib().mcrt_batch_read(self.h, int(i), dptr(A), dptr(Irt), dptr(Icb), dptr(lad), C.byref(st)))
+        irt, icb, ld = _views(cfg, Irt, Icb, lad)
+        return {"A": A, "Irt": irt, "Icb": icb, "ladder": ld, "stats": st.as_dict()}
+
+    def timing(self) -> Tuple[float, float]:
+        ms = np.zeros(1)
+        ph = np.zeros(1)
+        check(lib().mcrt_batch_timing(self.h, dptr(ms), dptr(ph)))
+        return float(ms[0]), float(ph[0])
+
+    def close(self) -> None:
+        if self.h:
+            lib().mcrt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ run_rt
+def _first_polarisation(I) -> Tuple[int, float]:
+    for j1 in range(1, 4):  # MonteCarloRadiativeTransfer.jl:208-215
+        if abs(I[j1]) > 1.0 - np.finfo(float).eps:
+            return j1, float(I[j1])
+    return 0, 0.0
+
+
+def run_rt(cfg, g, *, use_gpu: bool = True, ctx: Optional[Context] = None, **opts):
+    """run_rt (src/MonteCarloRadiativeTransfer.jl:87-291): the Mueller matrices of the
+    reflected (RT) and coherently backscattered (CB) light, as dicts of columns
+    ``theta`` (and ``phi`` for a plane), ``s11`` ... ``s44``, plus an ``energy`` dict.
+
+    Each incident polarisation state is one simulate() call with its own Philox key
+    word (``instance`` = state index)."""
+    g.validate()
+    IS = g.initial_I()
+    seed = opts.pop("seed", 1)
+    if g.kind == _lib.SPHERE:
+        return _run_rt_sphere(cfg, g, IS, seed, use_gpu, ctx, opts)
+    return _run_rt_plane(cfg, g, IS, seed, use_gpu, ctx, opts)
+
+
+def _run_rt_sphere(cfg, g, IS, seed, use_gpu, ctx, opts):
+    Nphi, Nphib = cfg.Nphi, cfg.Nphib
+    NFI = [i * Nphi // 8 for i in range(8)]
+    NFIB = [i * Nphib // 8 for i in range(8)]
+    G = np.zeros(4)  # dt, abs, ref, rem
+    MRT = np.zeros((4, 4, cfg.Ntheta))
+    MCB = np.zeros((4, 4, cfg.Nthetab))
+    for i in range(IS.shape[1]):
+        I = IS[:, i]
+        Adt, Aabs, Aref, _, Arem, IRT, ICB = simulate(cfg, g, I, use_gpu=use_gpu, ctx=ctx, seed=seed,
+                                                      instance=i, **opts)
+        if I[3] == 0:
+            G += [Adt, Aabs, Aref, Arem]
+            for M, X, N in ((MRT, IRT, NFI), (MCB, ICB, NFIB)):
+                M[:, 0, :] += (X[:, :, N[0]] + X[:, :, N[2]] + X[:, :, N[4]] + X[:, :, N[6]]) * 0.25
+                M[:, 1, :] += (-X[:, :, N[0]] + X[:, :, N[2]] - X[:, :, N[4]] + X[:, :, N[6]]) * 0.25
+                M[:, 2, :] += (X[:, :, N[1]] - X[:, :, N[3]] + X[:, :, N[5]] - X[:, :, N[7]]) * 0.25
+        else:
+            for M, X, N, n in ((MRT, IRT, NFI, Nphi), (MCB, ICB, NFIB, Nphib)):
+                M[2, 3, :] -= (X[2, :, N[0]] + X[2, :, N[4]]) * 0.5
+                M[3, 3, :] -= X[3, :, :].sum(axis=1) / n
+    Gsca = G[0] + G[2]
+    renorm = 1.0 / Gsca
+    MRT *= renorm * (1.0 / cfg.inorm)[None, None, :]
+    MCB *= renorm
+    sm_rt = {"theta": 180.0 / math.pi * np.arccos(cfg.costheta)}
+    sm_cb = {"theta": 180.0 / math.pi * np.arccos(cfg.costhetab)}
+    for a in range(4):
+        for b in range(4):
+            sm_rt[f"s{a + 1}{b + 1}"] = MRT[a, b, :].copy()
+            sm_cb[f"s{a + 1}{b + 1}"] = MCB[a, b, :].copy()
+    energy = {"direct_transmission": G[0], "absorption": G[1], "reflection": G[2], "remaining": G[3]}
+    return sm_rt, sm_cb, energy
+
+
+def _run_rt_plane(cfg, g, IS, seed, use_gpu, ctx, opts):
+    G = np.zeros(5)
+    MRT = np.zeros((4, 4, cfg.Ntheta, cfg.Nphi))
+    MCB = np.zeros((4, 4, cfg.Nthetab, cfg.Nphib))
+    for i in range(IS.shape[1]):
+        I = IS[:, i]
+        Adt, Aabs, Aref, Atrans, Arem, IRT, ICB = simulate(cfg, g, I, use_gpu=use_gpu, ctx=ctx, seed=seed,
+                                                           instance=i, **opts)
+        k1, k2 = _first_polarisation(I)
+        if k1 == 1:
+            G += np.array([Adt, Aabs, Aref, Atrans, Arem]) / 2.0
+            MRT[:, 0] += IRT / 2.0
+            MCB[:, 0] += ICB / 2.0
+        MRT[:, k1] += k2 * IRT / 2.0
+        MCB[:, k1] += k2 * ICB / 2.0
+    norm = np.abs(1.0 / (4.0 * cfg.costheta * cfg.inorm))  # MonteCarloRadiativeTransfer.jl:259
+    MRT *= norm[None, None, :, None]
+    norm1 = 1.0 / np.abs(4.0 * cfg.costhetab)  # :273-278
+    MCB *= norm1[None, None, :, None]
+    th = 180.0 / math.pi * np.arccos(cfg.costheta)
+    thb = 180.0 / math.pi * np.arccos(cfg.costhetab)
+    sm_rt = {"theta": np.tile(th, cfg.Nphi), "phi": np.repeat(180.0 / math.pi * cfg.phi, cfg.Ntheta)}
+    sm_cb = {"theta": np.tile(thb, cfg.Nphib), "phi": np.repeat(180.0 / math.pi * cfg.phib, cfg.Nthetab)}
+    for a in range(4):
+        for b in range(4):
+            sm_rt[f"s{a + 1}{b + 1}"] = MRT[a, b].reshape(-1, order="F").copy()
+            sm_cb[f"s{a + 1}{b + 1}"] = MCB[a, b].reshape(-1, order="F").copy()
+    energy = {"direct_transmission": G[0], "absorption": G[1], "reflection": G[2], "transmission": G[3],
+              "remaining": G[4]}
+    return sm_rt, sm_cb, energy
