@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Photon paths/s of the polarised Monte Carlo transport with coherent backscattering.
+
+Workload (one GPU): Mie spheres of size parameter 5 and refractive index 1.5+0.001i
+(1801-angle tables stored in FP32), a plane slab of optical thickness 5 with the Mie
+albedo, incidence zenith angle 30 degrees, unpolarised light, the reference's default
+bin grids, FP32 transport with FP64 CB phase reduction and FP64 tallies. One step is
+one persistent launch over a batch of photons; the full workload is 1e8 photons.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line. ``value`` is device-timed throughput with the inputs resident;
+``e2e`` is the same metric through the C ABI call mcrt_simulate with host buffers.
+With N > 1 (torchrun, one rank per GPU) the photon ranges are sharded across ranks
+with no collective in the data path (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "montecarloradiativetransfer.jl_gb300"))
+
+WORKLOAD = "mie_x5_m1.5+0.001i_slab_tau5_zenith30"
+TOTAL_PHOTONS = 100_000_000
+# FP32 flops per bin evaluation of the persistent kernel's formulation, counted by
+# hand from csrc/mcrt_transport.cuh with FMA = 2 flops (SFU operations not counted):
+# RT peel-off bin with a Mie lookup, CB reciprocal-path bin, CB single-scattering bin.
+FLOPS_RT_MIE = 98.0
+FLOPS_CBN_MIE = 330.0
+FLOPS_CB1_MIE = 110.0
+# DRAM bytes per launch of the transport kernel from ncu (scaled per photon from a
+# small capture); None until a capture has been summarised.
+NCU_DRAM_BYTES_PER_PHOTON = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=1 << 22, help="photons per step per GPU")
+    ap.add_argument("--fp64-sample", type=int, default=1 << 16)
+    ap.add_argument("--cpu-sample", type=int, default=2000)
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 and CPU legs")
+    return ap.parse_args()
+
+
+def workload(M, n_rays):
+    mie = M.MieScatterer(5.0 / (2 * math.pi), 1.5 + 0.001j, 1.0, 0.1, Ntheta=1801)
+    g = M.PlaneGeometry(math.radians(150.0), 0.0, [M.Layer(d=5.0 * mie.kl, scatterer=mie)])
+    cfg = M.Config(g, number_of_rays=n_rays)
+    return mie, g, cfg
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        top = max(sm)
+        loaded = [s for s in sm if s >= 0.5 * top] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_rate(M, n_sample, threads=0):
+    """Times the oracle (the FP64 C++ restatement of the reference's CPU path) on a bounded
+    sample of the same workload with all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    mie, g, cfg = workload(M, n_sample)
+    O.lib()
+    t0 = time.perf_counter()
+    O.simulate(cfg, g, [1.0, 0.0, 0.0, 0.0], seed=11, threads=threads)
+    dt = time.perf_counter() - t0
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return n_sample / dt, cores, dt
+
+
+def run_reference(args, rank):
+    """The reference arm: the reference's CPU algorithm (as the FP64 C++ oracle port,
+    since Julia is not installed) on the machine's host cores, same workload and metric."""
+    if rank != 0:
+        return
+    import mcrt_gb300 as M
+
+    rates = []
+    for _ in range(max(args.warmup, 0)):
+        cpu_oracle_rate(M, max(args.cpu_sample // 4, 100))
+    for _ in range(args.steps):
+        r, cores, dt = cpu_oracle_rate(M, args.cpu_sample)
+        rates.append(r)
+    v = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": "photon_paths_per_s", "value": v, "unit": "paths/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "photons_per_step": args.cpu_sample, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "paths/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.cpu_sample} photons per step of the same workload"},
+        "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Julia is not installed here, so the reference's CPU path runs as its FP64 C++ "
+                "restatement (oracle/mcrt_oracle.cpp) with OpenMP over photons",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import torch
+    import mcrt_gb300 as M
+
+    ctx = M.Context(local)
+    mie, g, cfg = workload(M, args.batch)
+    B = args.batch
+    I0 = [1.0, 0.0, 0.0, 0.0]
+    solve = M.Solve(cfg, g, I0, ctx=ctx, precision="fp32", seed=2)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    step_photons = lambda s: (s * world + rank) * B  # photon_begin of this rank's shard
+    for s in range(args.warmup):
+        solve.launch(step_photons(s), B)
+        solve.read()
+    clocks = Clocks(local)
+    barrier()
+    kms, stats = [], []
+    wall0 = time.perf_counter()
+    for s in range(args.steps):
+        flush.fill_(s & 0xFF)  # evict L2 between timed steps (outside the kernel's events)
+        torch.cuda.synchronize()
+        solve.launch(step_photons(args.warmup + s), B)
+        r = solve.read()
+        kms.append(r["stats"]["kernel_ms"])
+        stats.append(r["stats"])
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    t_dev = sum(kms) / 1e3
+    if dist:
+        t = torch.tensor([t_dev], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = world * B * args.steps / t_dev
+
+    # ---- e2e: the drop-in call with host buffers (uploads, launch, copy back, free)
+    e2e_times = []
+    h2d = d2h = 0
+    for s in range(args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        out = M.simulate(cfg, g, I0, ctx=ctx, precision="fp32", seed=3,
+                         photon_begin=step_photons(args.warmup + args.steps + s), with_extras=True)
+        e2e_times.append(time.perf_counter() - t0)
+    nrt, ncb = 4 * cfg.Ntheta * cfg.Nphi, 4 * cfg.Nthetab * cfg.Nphib
+    d2h = 8 * (nrt + ncb + ncb // 4 + 16)
+    h2d = 8 * (2 * cfg.Ntheta * 4 + 2 * cfg.Nphi + cfg.Nthetab * cfg.Nphib * 12 + 2 * cfg.Nthetab
+               + 2 * cfg.Nphib) // 2 + 2048  # FP32 bin tables + the instance descriptor
+    e2e_t = sum(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_t], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = {"value": world * B * args.steps / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "call": "mcrt_simulate (C ABI, host buffers)"}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ---- CB peak variance -> paths needed for 1% relative standard error
+    S = sum(st["cb_peak_sum"] for st in stats)
+    SS = sum(st["cb_peak_sumsq"] for st in stats)
+    N = sum(st["photons"] for st in stats)
+    mu = S / N
+    var = max(SS / N - mu * mu, 0.0)
+    paths_1pct = var / (0.01 * mu) ** 2 if mu > 0 else float("inf")
+    events = sum(st["events"] for st in stats)
+    rt = sum(st["rt_evals"] for st in stats)
+    cb1 = sum(st["cb1_evals"] for st in stats)
+    cbn = sum(st["cbn_evals"] for st in stats)
+    flops = rt * FLOPS_RT_MIE + cbn * FLOPS_CBN_MIE + cb1 * FLOPS_CB1_MIE
+    achieved = flops / t_dev / 1e12 / world
+    peak = ctx.fp32_peak_tflops()
+    traffic = None
+    if NCU_DRAM_BYTES_PER_PHOTON is not None:
+        traffic = NCU_DRAM_BYTES_PER_PHOTON * B
+
+    extras = {}
+    if not args.no_extras:
+        # FP64 forms on bounded samples: the same persistent kernel in FP64, and the plain
+        # per-ray FP64 kernel with the reference's structure (denominator of the 5x target).
+        n64 = args.fp64_sample
+        _, g64, cfg64 = workload(M, n64)
+        np64 = 4 * n64
+        s64 = M.Solve(cfg64.replace(number_of_rays=np64), g64, I0, ctx=ctx, precision="fp64", seed=2)
+        s64.launch(0, np64)
+        r64 = s64.read()
+        s64.close()
+        plain_threads = min(n64, 65536)
+        sp = M.Solve(cfg64.replace(maximum_threads=plain_threads), g64, I0, ctx=ctx, precision="fp64",
+                     kernel="plain", seed=2)
+        sp.launch(0, n64)
+        rp = sp.read()
+        sp.close()
+        v64 = np64 / (r64["stats"]["kernel_ms"] / 1e3)
+        vplain = n64 / (rp["stats"]["kernel_ms"] / 1e3)
+        cpu_v, cores, cpu_dt = cpu_oracle_rate(M, args.cpu_sample)
+        extras = {
+            "fp64_persistent": {"value": v64, "unit": "paths/s", "sample_photons": np64},
+            "fp64_plain": {"value": vplain, "unit": "paths/s", "sample_photons": n64,
+                           "threads": plain_threads},
+            "fp32_over_fp64_plain": value / world / vplain,
+            "fp32_over_fp64_persistent": value / world / v64,
+            "cpu_baseline": {"value": cpu_v, "unit": "paths/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.cpu_sample} photons of the same workload, FP64, "
+                                       f"{cpu_dt:.1f} s"},
+        }
+
+    line = {
+        "metric": "photon_paths_per_s", "value": value, "unit": "paths/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": B, "total_photons": TOTAL_PHOTONS,
+                   "bins": {"Ntheta": cfg.Ntheta, "Nphi": cfg.Nphi, "Ntheta_b": cfg.Nthetab,
+                            "Nphi_b": cfg.Nphib},
+                   "mie_table_angles": 1801, "parallelism": f"photon shards x{world}",
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "launch": {"block_size": stats[0]["block_size"], "blocks": stats[0]["blocks"]}},
+        "e2e": e2e,
+        "gpu_launches": args.steps,
+        "wall_s_timed": wall,
+        "cb_peak": {"mean_per_path": mu, "std_per_path": math.sqrt(var),
+                    "paths_for_1pct_stderr": paths_1pct,
+                    "seconds_to_1pct_fp32": paths_1pct / value},
+        "events_per_path": events / N,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "live FP32 FFMA microbenchmark (mcrt_measure_fp32_peak)",
+                     "flops_per_unit": {"rt_bin": FLOPS_RT_MIE, "cb_reciprocal_bin": FLOPS_CBN_MIE,
+                                        "cb_single_bin": FLOPS_CB1_MIE}},
+        "clocks": clk,
+    }
+    line.update(extras)
+    if "fp64_plain" in extras:
+        line["cb_peak"]["seconds_to_1pct_fp64_plain"] = paths_1pct / extras["fp64_plain"]["value"]
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

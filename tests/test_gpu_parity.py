@@ -1,0 +1,248 @@
+"""GPU parity tests: the CUDA kernels (through the C ABI) against the CPU oracle.
+
+Tolerances (scaled errors as defined in helpers.scaled_err):
+  * FP64 kernels vs the FP64 oracle on identical Philox streams: 1e-9 on every tally
+    (both restate the same arithmetic; only rounding order differs).
+  * FP32 persistent kernel vs its FP64 form on identical streams: 1e-4 on every tally.
+  * Independent streams: every Stokes element within 3 combined Monte Carlo standard
+    errors (batch means), allowing the 1% of elements that a 3-sigma band misses by
+    chance, and none beyond 5 sigma; the CB enhancement within 3 sigma.
+  * First scattering order vs the analytic single-scattering slab result: 1e-6 (FP64),
+    1e-5 (FP32).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import cb_peak_stats, scaled_err, sim_arrays
+
+pytestmark = pytest.mark.gpu
+N0 = [1.0, 0.0, 0.0, 0.0]
+
+
+def small_cfg(M, g, n, **kw):
+    kw.setdefault("Ntheta", 16)
+    kw.setdefault("Nphi", 8)
+    kw.setdefault("Nphib", 4)
+    kw.setdefault("thetab", np.deg2rad(np.linspace(0, 3, 12)))
+    kw.setdefault("maximum_scattering_times", 500)
+    return M.Config(g, number_of_rays=n, **kw)
+
+
+def geometry(M, case, mie5, mie2):
+    ray = M.RayleighScatterer(0.99, 100.0)
+    if case == "plane_rayleigh":
+        return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), N0
+    if case == "plane_rayleigh_V":
+        return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), [1, 0, 0, -1]
+    if case == "plane_mie_oblique":
+        return M.PlaneGeometry(math.radians(150), 0.4, [M.Layer(d=3 * mie5.kl, scatterer=mie5)]), [1, 0, 1, 0]
+    if case == "sphere_mie":
+        return M.SphereGeometry(R=6 * mie2.kl, scatterer=mie2), N0
+    if case == "two_layers":
+        return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1 * ray.kl, scatterer=ray),
+                                              M.Layer(d=2 * mie5.kl, scatterer=mie5)]), N0
+    if case == "semi_infinite":
+        return M.PlaneGeometry(math.radians(170), 0.0, [M.Layer(d=1 * ray.kl, scatterer=ray),
+                                                        M.Layer(d=-1.0, scatterer=ray, tau=math.inf)]), [1, 1, 0, 0]
+    raise ValueError(case)
+
+
+CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_kernels_match_oracle_on_same_streams(M, O, gpu_ctx, mie5, mie2, case):
+    g, I0 = geometry(M, case, mie5, mie2)
+    cfg = small_cfg(M, g, 600)
+    n = cfg.number_of_rays
+    ref = O.simulate(cfg, g, I0, seed=21, threads=0)
+    for kernel in ("persistent", "plain"):
+        out = M.simulate(cfg, g, I0, precision="fp64", kernel=kernel, seed=21, with_extras=True)
+        A, Irt, Icb = sim_arrays(out)
+        st = out[7]["stats"]
+        assert st["status_flags"] & 5 == 0
+        assert st["photons"] == n
+        assert st["events"] == ref["counters"]["events"], kernel
+        assert scaled_err(A, ref["A"] / n) < 1e-9, kernel
+        assert scaled_err(Irt, ref["Irt"] / n) < 1e-9, kernel
+        assert scaled_err(Icb, ref["Icb"] / n) < 1e-9, kernel
+        assert scaled_err(out[7]["ladder"], ref["ladder"] / n) < 1e-9, kernel
+        if ref["stats"]["cb_peak_sum"] != 0:
+            assert abs(st["cb_peak_sum"] / ref["stats"]["cb_peak_sum"] - 1) < 1e-9
+        assert abs(A.sum() - 1) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["plane_rayleigh", "plane_mie_oblique", "sphere_mie"])
+def test_fp32_matches_fp64_on_same_streams(M, gpu_ctx, mie5, mie2, case):
+    g, I0 = geometry(M, case, mie5, mie2)
+    cfg = small_cfg(M, g, 1 << 14)
+    o64 = M.simulate(cfg, g, I0, precision="fp64", seed=5, with_extras=True)
+    o32 = M.simulate(cfg, g, I0, precision="fp32", seed=5, with_extras=True)
+    A64, R64, C64 = sim_arrays(o64)
+    A32, R32, C32 = sim_arrays(o32)
+    errs = {"A": scaled_err(A32, A64), "Irt": scaled_err(R32, R64), "Icb": scaled_err(C32, C64),
+            "ladder": scaled_err(o32[7]["ladder"], o64[7]["ladder"])}
+    print(case, "FP32 vs FP64 scaled errors:", errs)
+    for k, e in errs.items():
+        assert e < 1e-4, (k, e)
+    assert abs(A32.sum() - 1) < 1e-5
+
+
+def _batch_means(M, cfg, g, I0, prec, seed, nb):
+    """nb independent sub-runs on consecutive photon ranges of one stream."""
+    n = cfg.number_of_rays
+    s = M.Solve(cfg, g, I0, precision=prec, seed=seed)
+    outs = []
+    for b in range(nb):
+        s.launch(b * n, n)
+        r = s.read()
+        outs.append((r["Irt"] / n, r["Icb"] / n, r["ladder"] / n))
+    s.close()
+    return [np.array([o[i] for o in outs]) for i in range(3)]
+
+
+def test_statistics_agree_with_oracle_on_independent_streams(M, O, gpu_ctx):
+    ray = M.RayleighScatterer(0.99, 100.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=4 * ray.kl, scatterer=ray)])
+    cfg = small_cfg(M, g, 2000)
+    nb = 16
+    R, C, L = _batch_means(M, cfg, g, N0, "fp32", 101, nb)
+    ref = O.simulate(cfg.replace(number_of_rays=4 * cfg.number_of_rays), g, N0, seed=202, threads=0)
+    nr = 4 * cfg.number_of_rays
+    gpu_mean = R.mean(0)
+    se_gpu = R.std(0, ddof=1) / math.sqrt(nb)
+    se_ref = R.std(0, ddof=1) * math.sqrt(cfg.number_of_rays / nr)  # same per-path variance
+    se = np.sqrt(se_gpu ** 2 + se_ref ** 2)
+    d = np.abs(gpu_mean - ref["Irt"] / nr)
+    mask = se > 0
+    z = d[mask] / se[mask]
+    assert np.mean(z > 3) < 0.01, np.mean(z > 3)
+    assert z.max() < 5.5, z.max()
+    # CB enhancement factor at exact backscatter: s11 of Icb over the ladder at theta_b = 0
+    enh = C[:, 0, 0, 0] / L[:, 0, 0]
+    enh_ref = ref["Icb"][0, 0, 0] / ref["ladder"][0, 0]
+    se_e = enh.std(ddof=1) / math.sqrt(nb) * math.sqrt(1 + cfg.number_of_rays * nb / nr)
+    assert abs(enh.mean() - enh_ref) < 3 * se_e, (enh.mean(), enh_ref, se_e)
+    assert 1.0 < enh_ref <= 2.0
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-6), ("fp32", 1e-5)])
+def test_first_order_matches_analytic_single_scattering(M, gpu_ctx, prec, tol):
+    ray = M.RayleighScatterer(0.9, 1.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0, scatterer=ray)])
+    cfg = small_cfg(M, g, 1 << 16, maximum_scattering_times=1)
+    out = M.simulate(cfg, g, N0, precision=prec, seed=3, rng_mode=1)
+    got = out[5][0]
+    tau, mu0 = 1.0, 1.0
+    exp = np.zeros_like(got)
+    for j1 in range(cfg.Ntheta):
+        mu = cfg.costheta[j1]
+        c = -mu  # cos of the scattering angle for normal incidence
+        if mu > 0:
+            f = mu * (1 - math.exp(-tau * (1 / mu0 + 1 / mu))) / (mu + mu0)
+        else:
+            a = 1 - mu0 / -mu
+            f = math.exp(-tau / -mu) * (1 - math.exp(-tau / mu0 * a)) / a
+        exp[j1, :] = 0.9 * 0.75 * (1 + c * c) * cfg.inorm[j1] * f
+    assert np.max(np.abs(got - exp) / exp) < tol
+    cb = out[6][0, 0, 0]
+    assert abs(cb / (0.9 * 1.5 * (1 - math.exp(-2.0)) / 2) - 1) < tol
+
+
+def test_batch_matches_individual_solves(M, gpu_ctx, mie5, mie2):
+    ray = M.RayleighScatterer(0.95, 50.0)
+    geos = [(M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=2 * ray.kl, scatterer=ray)]), N0, 3000),
+            (M.PlaneGeometry(math.radians(140), 1.0, [M.Layer(d=1 * mie5.kl, scatterer=mie5)]), [1, 0, 0, 1], 500),
+            (M.SphereGeometry(R=2 * mie2.kl, scatterer=mie2), N0, 1200),
+            (M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=0.3 * ray.kl, scatterer=ray)]), [1, -1, 0, 0], 7)]
+    cfg = small_cfg(M, geos[0][0], 1)
+    inst = [{"geometry": g, "I0": I, "n_photons": n, "seed": 40 + i, "instance": i}
+            for i, (g, I, n) in enumerate(geos)]
+    b = M.Batch(cfg, inst, precision="fp64")
+    b.launch()
+    for i, (g, I, n) in enumerate(geos):
+        r = b.read(i)
+        # the batch shares the config's bin grids, so the solo run reuses the same arrays
+        solo = M.simulate(cfg.replace(number_of_rays=n), g, I, precision="fp64", seed=40 + i,
+                          instance=i, with_extras=True)
+        assert r["stats"]["photons"] == n
+        assert scaled_err(r["A"] / n, np.array(solo[:5])) < 1e-12
+        assert scaled_err(r["Irt"] / n, solo[5]) < 1e-12
+        assert scaled_err(r["Icb"] / n, solo[6]) < 1e-12
+    b.close()
+
+
+def test_edge_cases(M, gpu_ctx, mie5):
+    ray = M.RayleighScatterer(0.99, 10.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=3 * ray.kl, scatterer=ray)])
+    # zero photons: all-zero tallies
+    out = M.simulate(small_cfg(M, g, 0), g, N0, with_extras=True)
+    assert np.all(np.array(out[:5]) == 0) and not np.any(out[5]) and not np.any(out[6])
+    # one photon and an odd count
+    for n in (1, 37):
+        out = M.simulate(small_cfg(M, g, n), g, N0, precision="fp64", with_extras=True)
+        assert abs(sum(out[:5]) - 1) < 1e-12 and out[7]["stats"]["photons"] == n
+    # no CB: the CB tallies stay zero, RT unchanged
+    a = M.simulate(small_cfg(M, g, 300), g, N0, precision="fp64", seed=4)
+    b = M.simulate(small_cfg(M, g, 300, compute_cb=False), g, N0, precision="fp64", seed=4)
+    assert not np.any(b[6]) and scaled_err(b[5], a[5]) < 1e-12
+    # no scattering allowed: only direct transmission and the remaining weight
+    out = M.simulate(small_cfg(M, g, 100, maximum_scattering_times=0), g, N0, precision="fp64")
+    assert out[1] == 0 and out[2] == 0 and not np.any(out[5])
+    assert abs(out[0] - math.exp(-3)) < 1e-12 and abs(out[4] - (1 - math.exp(-3))) < 1e-12
+    # optically very thin and very thick slabs (tau beyond tau0 disables the lower peel-off)
+    for tau in (0.01, 60.0):
+        gt = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=tau * ray.kl, scatterer=ray)])
+        out = M.simulate(small_cfg(M, gt, 200), gt, N0, precision="fp64", with_extras=True)
+        assert abs(sum(out[:5]) - 1) < 1e-12
+        assert out[7]["stats"]["status_flags"] & 5 == 0
+    # invalid input is rejected with the reference's message
+    bad = M.PlaneGeometry(1.0, 0.0, [M.Layer(d=1.0, scatterer=ray)])
+    with pytest.raises(ValueError, match="θ must be in"):
+        M.simulate(small_cfg(M, g, 10), bad, N0)
+
+
+def test_full_size_workload_properties(M, gpu_ctx, mie5):
+    """At the benchmark workload's size: size-independent properties of the result."""
+    g = M.PlaneGeometry(math.radians(150), 0.0, [M.Layer(d=5 * mie5.kl, scatterer=mie5)])
+    cfg = M.Config(g, number_of_rays=1 << 21)
+    out = M.simulate(cfg, g, N0, precision="fp32", seed=2, with_extras=True)
+    A = np.array(out[:5])
+    st = out[7]["stats"]
+    assert abs(A.sum() - 1) < 1e-5
+    assert st["photons"] == cfg.number_of_rays and st["status_flags"] & 5 == 0
+    assert np.all(np.isfinite(out[5])) and np.all(np.isfinite(out[6]))
+    assert np.all(out[5][0] >= 0) and np.all(out[7]["ladder"] >= 0)
+    enh = out[6][0, 0, 0] / out[7]["ladder"][0, 0]
+    assert 1.0 < enh <= 2.0
+    mu, sd = cb_peak_stats(st)
+    assert mu > 0 and abs(mu - out[6][0, 0, 0]) < 1e-6 * mu
+    # splitting the photons into two launches on the same stream gives the same sums
+    s = M.Solve(cfg, g, N0, precision="fp32", seed=2)
+    half = cfg.number_of_rays // 2
+    s.launch(0, half)
+    r1 = s.read()
+    s.launch(half, half)
+    r2 = s.read()
+    s.close()
+    tot = (r1["Irt"] + r2["Irt"]) / cfg.number_of_rays
+    assert scaled_err(tot, out[5]) < 1e-6
+
+
+def test_run_rt_on_gpu(M, gpu_ctx, mie2):
+    ray = M.RayleighScatterer(0.99, 100.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=2 * ray.kl, scatterer=ray)])
+    cfg = small_cfg(M, g, 2000)
+    sm_rt, sm_cb, energy = M.run_rt(cfg, g)
+    assert len(sm_rt["s11"]) == cfg.Ntheta * cfg.Nphi
+    assert np.all(np.isfinite(sm_rt["s11"]))
+    up = cfg.costheta > 0
+    s11 = sm_rt["s11"].reshape(cfg.Nphi, cfg.Ntheta).T
+    assert np.all(s11[up] > 0)
+    assert abs(sum(energy.values()) - 1) < 1e-5
+    gs = M.SphereGeometry(R=2 * mie2.kl, scatterer=mie2)
+    cs = small_cfg(M, gs, 2000)
+    sm_rt, sm_cb, energy = M.run_rt(cs, gs)
+    assert np.all(np.isfinite(sm_rt["s11"])) and np.all(sm_rt["s11"] > 0)

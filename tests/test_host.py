@@ -1,0 +1,180 @@
+"""CPU tests of the library's host side: the exported C ABI, the Mie table producer,
+Config defaults and quadratures, validation, and the run_rt Mueller assembly."""
+import json
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "mcrt.h")).read()
+    return sorted(set(re.findall(r"\b(mcrt_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(M):
+    L = M.lib()
+    syms = header_symbols()
+    assert len(syms) >= 19
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) <= set(M._lib.SIGNATURES), "ctypes signatures missing for: %s" % (
+        set(syms) - set(M._lib.SIGNATURES))
+    assert L.mcrt_abi_version() == 1
+
+
+def test_no_device_is_reported_not_faked(M):
+    # Without a GPU the library must refuse to compute rather than fall back to a CPU path.
+    L = M.lib()
+    if L.mcrt_device_count() > 0:
+        pytest.skip("a GPU is visible")
+    import ctypes
+
+    h = ctypes.c_void_p()
+    assert L.mcrt_ctx_create(0, ctypes.byref(h)) == M._lib.MCRT_ENODEV
+    with pytest.raises(M.MCRTError):
+        M.Context(0)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_mie_tables_match_an_independent_mie_evaluation(M, case):
+    c = json.load(open(os.path.join(GOLDEN, "mie_scipy.json")))[case]
+    x, m = c["x"], complex(*c["m"])
+    ang = np.array(c["angles_deg"])
+    # Angles 0, 30, ..., 180 lie on the uniform grid of 7 points.
+    s = M.MieScatterer(x / (2 * math.pi), m, 1.0, 0.1, Ntheta=7)
+    assert np.allclose(np.rad2deg(np.linspace(0, math.pi, 7)), ang)
+    assert abs(s.q_ext / c["q_ext"] - 1) < 1e-10
+    assert abs(s.q_sca / c["q_sca"] - 1) < 1e-10
+    assert abs(s.asymm / c["asymm"] - 1) < 1e-9
+    S1 = np.array([complex(*v) for v in c["S1"]])
+    S2 = np.array([complex(*v) for v in c["S2"]])
+    assert np.max(np.abs(s.S11 - S1)) < 1e-10 * np.max(np.abs(S1))
+    assert np.max(np.abs(s.S22 - S2)) < 1e-10 * np.max(np.abs(S2))
+    assert abs(s.omega - c["q_sca"] / c["q_ext"]) < 1e-10  # mie.jl:39
+
+
+def test_mie_phase_function_is_normalised_and_csrn_is_an_inverse_cdf(M, mie5):
+    th = np.linspace(0, math.pi, mie5.Ntheta)
+    assert abs(np.trapezoid(mie5.F11 * np.sin(th), th) / 2 - 1) < 1e-4
+    cs = mie5.csrn
+    assert len(cs) == 1001
+    assert np.all(np.diff(cs) >= 0)
+    assert cs[-1] == 1.0 and -1.0 <= cs[0] < -0.99
+    # the median of cos(theta) under F11 sin(theta)
+    cdf = np.cumsum(mie5.F11 * np.sin(th))
+    cdf /= cdf[-1]
+    med = math.cos(th[np.searchsorted(cdf, 0.5)])
+    assert abs(cs[500] - med) < 0.01
+    assert abs(mie5.kl - (4 / 3) * mie5.r / (mie5.nu * mie5.q_ext)) < 1e-12  # mie.jl:40
+
+
+def test_config_defaults_mirror_the_reference(M):
+    ray = M.RayleighScatterer(0.99, 1.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=10.0, scatterer=ray)])
+    cfg = M.Config(g)
+    assert (cfg.number_of_rays, cfg.minimum_intensity, cfg.maximum_scattering_times) == (1000, 1e-6, 10000)
+    assert (cfg.maximum_threads, cfg.compute_cb, cfg.tau0) == (8192, True, 50.0)
+    assert (cfg.Nphi, cfg.Ntheta, cfg.Nthetab, cfg.Nphib) == (48, 64, 51, 8)
+    assert abs(cfg.thetab[-1] - math.pi) < 1e-15 and cfg.thetab[0] == 0.0
+    assert abs(cfg.phi[1] - 2 * math.pi / 48) < 1e-15
+    # half-range Gauss-Legendre: each hemisphere's inorm sums to 1 / (2 Nphi) * 1
+    h = cfg.Ntheta // 2
+    assert np.all(cfg.costheta[:h] < 0) and np.all(cfg.costheta[h:] > 0)
+    assert abs(cfg.inorm[:h].sum() * 2 * cfg.Nphi - 1) < 1e-14
+    assert abs(np.sum(cfg.inorm[h:] * cfg.costheta[h:]) * 2 * cfg.Nphi - 0.5) < 1e-14
+    s = M.SphereGeometry(R=2.0, scatterer=ray)
+    cs = M.Config(s)
+    assert abs(cs.inorm.sum() * 2 * cs.Nphi - 2) < 1e-14
+    assert s.tau == 2.0 and s.omega == 0.99
+    assert g.layers[0].tau == 10.0 and not g.layers[0].infinite
+
+
+def test_validation_messages(M):
+    ray = M.RayleighScatterer(0.99, 1.0)
+    with pytest.raises(ValueError, match="θ must be in"):
+        M.PlaneGeometry(1.0, 0.0, [M.Layer(d=1.0, scatterer=ray)]).validate()
+    with pytest.raises(ValueError, match="ϕ must be in"):
+        M.PlaneGeometry(math.pi, 7.0, [M.Layer(d=1.0, scatterer=ray)]).validate()
+    with pytest.raises(ValueError, match="at least one layer"):
+        M.PlaneGeometry(math.pi, 0.0, []).validate()
+    with pytest.raises(ValueError, match="Only the last layer"):
+        M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=-1, scatterer=ray, tau=math.inf),
+                                       M.Layer(d=1, scatterer=ray)]).validate()
+    with pytest.raises(ValueError, match="Radius must be positive"):
+        M.SphereGeometry(R=0.0, scatterer=ray).validate()
+
+
+def test_cpu_path_is_not_offered(M):
+    ray = M.RayleighScatterer(0.99, 1.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0, scatterer=ray)])
+    with pytest.raises(NotImplementedError):
+        M.simulate(M.Config(g), g, [1, 0, 0, 0], use_gpu=False)
+
+
+def _fake_simulate(calls):
+    """A stand-in for simulate() returning tallies that encode the incident state."""
+
+    def sim(cfg, g, I, **kw):
+        calls.append(np.array(I))
+        k = len(calls)
+        irt = np.zeros((4, cfg.Ntheta, cfg.Nphi))
+        icb = np.zeros((4, cfg.Nthetab, cfg.Nphib))
+        for s in range(4):
+            irt[s] = (s + 1) * 10.0 ** k + np.arange(cfg.Ntheta)[:, None] + 0.1 * np.arange(cfg.Nphi)[None, :]
+            icb[s] = (s + 1) * 10.0 ** k + np.arange(cfg.Nthetab)[:, None]
+        return 0.1 * k, 0.2, 0.3, 0.05, 0.01, irt, icb
+
+    return sim
+
+
+def test_run_rt_plane_assembly(M, monkeypatch):
+    """The plane Mueller assembly of MonteCarloRadiativeTransfer.jl:186-291."""
+    from mcrt_gb300 import engine
+
+    calls = []
+    monkeypatch.setattr(engine, "simulate", _fake_simulate(calls))
+    ray = M.RayleighScatterer(0.99, 1.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0, scatterer=ray)])
+    cfg = M.Config(g, Ntheta=4, Nphi=2, Nphib=2, thetab=[0.0, 0.1, math.pi / 2])
+    sm_rt, sm_cb, energy = M.run_rt(cfg, g)
+    assert len(calls) == 6
+    # column 1 = (R(-Q) + R(+Q)) / 2, column 2 = (R(+Q) - R(-Q)) / 2 of the raw tallies
+    norm = np.abs(1 / (4 * cfg.costheta * cfg.inorm))
+    s11 = sm_rt["s11"].reshape(cfg.Nphi, cfg.Ntheta).T
+    s12 = sm_rt["s12"].reshape(cfg.Nphi, cfg.Ntheta).T
+    raw = lambda k, s: (s + 1) * 10.0 ** k + np.arange(cfg.Ntheta)[:, None] + 0.1 * np.arange(cfg.Nphi)[None, :]
+    assert np.allclose(s11, (raw(1, 0) + raw(2, 0)) / 2 * norm[:, None])
+    assert np.allclose(s12, (raw(2, 0) - raw(1, 0)) / 2 * norm[:, None])
+    s44 = sm_rt["s44"].reshape(cfg.Nphi, cfg.Ntheta).T
+    assert np.allclose(s44, (raw(6, 3) - raw(5, 3)) / 2 * norm[:, None])
+    assert np.allclose(sm_rt["theta"][: cfg.Ntheta], np.degrees(np.arccos(cfg.costheta)))
+    assert energy["direct_transmission"] == pytest.approx((0.1 + 0.2) / 2)
+    cb = sm_cb["s11"].reshape(cfg.Nphib, cfg.Nthetab).T
+    rawb = lambda k, s: (s + 1) * 10.0 ** k + np.arange(cfg.Nthetab)[:, None]
+    assert np.allclose(cb, (rawb(1, 0) + rawb(2, 0)) / 2 / np.abs(4 * cfg.costhetab)[:, None])
+
+
+def test_run_rt_sphere_assembly(M, monkeypatch):
+    """The sphere Mueller assembly of MonteCarloRadiativeTransfer.jl:87-184."""
+    from mcrt_gb300 import engine
+
+    calls = []
+    monkeypatch.setattr(engine, "simulate", _fake_simulate(calls))
+    ray = M.RayleighScatterer(0.99, 1.0)
+    g = M.SphereGeometry(R=1.0, scatterer=ray)
+    cfg = M.Config(g, Ntheta=4, Nphi=8, Nphib=8, thetab=[0.0, 0.1])
+    sm_rt, sm_cb, energy = M.run_rt(cfg, g)
+    assert len(calls) == 2
+    raw1 = lambda s, j2: (s + 1) * 10.0 + np.arange(cfg.Ntheta) + 0.1 * j2
+    renorm = 1 / (0.1 + 0.3)
+    exp11 = (raw1(0, 0) + raw1(0, 2) + raw1(0, 4) + raw1(0, 6)) * 0.25 * renorm / cfg.inorm
+    assert np.allclose(sm_rt["s11"], exp11)
+    exp44 = -np.mean([(4 * 100.0 + np.arange(cfg.Ntheta) + 0.1 * j2) for j2 in range(8)], axis=0)
+    assert np.allclose(sm_rt["s44"], exp44 * renorm / cfg.inorm)
+    assert energy["reflection"] == pytest.approx(0.3)

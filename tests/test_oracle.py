@@ -1,0 +1,166 @@
+"""Known-answer tests that pin the CPU oracle (oracle/mcrt_oracle.cpp) to the reference's
+semantics. The reference ships no golden vectors, so every expected value here is
+derived independently: published Philox vectors, closed forms, exact invariants."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from helpers import scaled_err
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+N0 = [1.0, 0.0, 0.0, 0.0]
+
+
+def test_philox_known_answers(O):
+    for kat in json.load(open(os.path.join(GOLDEN, "philox_kat.json"))):
+        assert O.philox(kat["ctr"], kat["key"]) == kat["out"]
+
+
+def test_rayleigh_sampler_inverts_the_phase_function_cdf(O):
+    # rayleigh.jl:10-11 maps u to cos(theta) with P11 ~ 3/8 (1 + mu^2); the sampled
+    # cosine c satisfies CDF(c) = 1 - u exactly (the density is symmetric).
+    cdf = lambda c: (3 * c + c ** 3 + 4) / 8
+    for u in np.linspace(1e-6, 1 - 1e-6, 2001):
+        c = O.lib().orc_rayleigh_sample(u)
+        assert abs(cdf(c) - (1 - u)) < 1e-12
+
+
+def test_kepler_solver_solves_keplers_equation(O):
+    rng = np.random.default_rng(0)
+    for M, e in zip(rng.uniform(-10, 20, 500), rng.uniform(0, 0.98, 500)):
+        E = O.lib().orc_kepler_solver(M, e)
+        assert abs(E - e * math.sin(E) - M) < 1e-10
+
+
+def _plane(M, s, tau, theta=math.pi, phi=0.0):
+    return M.PlaneGeometry(theta, phi, [M.Layer(d=tau * s.kl, scatterer=s)])
+
+
+def _small_cfg(M, g, n, **kw):
+    kw.setdefault("Ntheta", 16)
+    kw.setdefault("Nphi", 8)
+    kw.setdefault("Nphib", 4)
+    kw.setdefault("thetab", np.deg2rad(np.linspace(0, 3, 10)))
+    return M.Config(g, number_of_rays=n, **kw)
+
+
+@pytest.mark.parametrize("case", ["rayleigh", "rayleigh_Q", "rayleigh_V", "mie_oblique", "sphere",
+                                  "two_layers", "semi_infinite"])
+def test_energy_closure_and_cb_forms(M, O, mie5, mie2, case):
+    """Per photon the bookkeeping conserves I1 (src/gpu.jl:199-200,259-260,285-294), so
+    Adt + Aabs + Aref + Atrans + Arem = 1; and the incremental reciprocal-path fields
+    reproduce the reference's O(n) walks (src/utils.jl:199-241)."""
+    ray = M.RayleighScatterer(0.99, 100.0)
+    I0 = N0
+    if case.startswith("rayleigh"):
+        g = _plane(M, ray, 4.0)
+        I0 = {"rayleigh": N0, "rayleigh_Q": [1, 1, 0, 0], "rayleigh_V": [1, 0, 0, -1]}[case]
+    elif case == "mie_oblique":
+        g = _plane(M, mie5, 2.0, theta=math.radians(150.0), phi=0.3)
+    elif case == "sphere":
+        g = M.SphereGeometry(R=3.0 * mie2.kl, scatterer=mie2)
+    elif case == "two_layers":
+        g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0 * ray.kl, scatterer=ray),
+                                           M.Layer(d=2.0 * mie5.kl, scatterer=mie5)])
+    else:
+        g = M.PlaneGeometry(math.radians(160.0), 0.0, [M.Layer(d=1.0 * ray.kl, scatterer=ray),
+                                                      M.Layer(d=-1.0, scatterer=ray, tau=math.inf)])
+    cfg = _small_cfg(M, g, 150, maximum_scattering_times=300)
+    walk = O.simulate(cfg, g, I0, seed=5, cb_form=0, threads=4)
+    inc = O.simulate(cfg, g, I0, seed=5, cb_form=1, threads=4)
+    n = cfg.number_of_rays
+    assert walk["counters"]["attempts_capped"] == 0
+    assert abs(walk["A"].sum() / n - 1.0) < 1e-12
+    assert walk["stats"]["photons"] == n
+    assert scaled_err(inc["Icb"], walk["Icb"]) < 1e-12
+    assert scaled_err(inc["ladder"], walk["ladder"]) < 1e-12
+    # the RT tallies do not depend on the CB form; they differ only by the order in
+    # which the OpenMP threads' partial sums are added
+    assert scaled_err(inc["Irt"], walk["Irt"]) < 1e-13
+    assert np.max(np.abs(inc["A"] - walk["A"])) / n < 1e-13
+
+
+def _first_order(M, O, s, tau, theta0, P11, n=1 << 16):
+    g = _plane(M, s, tau, theta=theta0)
+    cfg = _small_cfg(M, g, n, maximum_scattering_times=1)
+    r = O.simulate(cfg, g, N0, seed=3, rng_mode=1, threads=0)
+    mu0 = abs(math.cos(theta0))
+    k0 = np.array([math.sin(theta0), 0.0, math.cos(theta0)])
+    got = r["Irt"][0] / n
+    exp = np.zeros_like(got)
+    for j1 in range(cfg.Ntheta):
+        mu = cfg.costheta[j1]
+        for j2 in range(cfg.Nphi):
+            k = np.array([cfg.sintheta[j1] * cfg.cosphi[j2], cfg.sintheta[j1] * cfg.sinphi[j2], mu])
+            c = float(np.dot(k0, k))
+            if mu > 0:  # reflection: depth |z| escapes along mu
+                f = mu * (1 - math.exp(-tau * (1 / mu0 + 1 / mu))) / (mu + mu0)
+            else:  # transmission through the rest of the slab
+                am = -mu
+                a = 1 - mu0 / am
+                f = math.exp(-tau / am) * ((1 - math.exp(-tau / mu0 * a)) / a if abs(a) > 1e-12 else tau / mu0)
+            exp[j1, j2] = s.omega * P11(c) * cfg.inorm[j1] * f
+    return got, exp, r, cfg
+
+
+def test_first_order_matches_single_scattering_rayleigh(M, O):
+    """maximum_scattering_times = 1 leaves only the first order, which must equal the
+    analytic single-scattering slab reflection and transmission
+    omega P11 [1 - exp(-tau (1/mu0 + 1/mu))] / (mu + mu0) (times mu and inorm, the
+    reference's normalisation), with the first-collision depth drawn on a midpoint grid."""
+    ray = M.RayleighScatterer(0.9, 1.0)
+    got, exp, r, cfg = _first_order(M, O, ray, 1.0, math.pi, lambda c: 0.75 * (1 + c * c))
+    assert np.max(np.abs(got - exp) / exp) < 1e-6
+    # Linear polarisation of singly scattered unpolarised light: Q^2 + U^2 = (P12 f)^2.
+    n = cfg.number_of_rays
+    Q, U = r["Irt"][1] / n, r["Irt"][2] / n
+    c = -cfg.costheta[:, None] * np.ones((1, cfg.Nphi))
+    p12 = -0.75 * (1 - c * c)
+    assert np.max(np.abs(np.sqrt(Q ** 2 + U ** 2) - np.abs(p12 / (0.75 * (1 + c * c)) * got))) < 1e-6 * got.max()
+    assert np.max(np.abs(r["Irt"][3])) == 0.0
+
+
+def test_first_order_matches_single_scattering_mie_oblique(M, O, mie5):
+    s = mie5.rounded_fp32()
+    nt = s.Ntheta
+
+    def P11(c):  # the reference's lerp on the uniform theta grid (mie.jl:53-66)
+        th = math.acos(max(-1.0, min(1.0, c)))
+        sn = th / math.pi * (nt - 1)
+        i = min(int(sn), nt - 1)
+        f = sn - i
+        v = (1 - f) * s.F11[i]
+        if i + 1 <= nt - 1:
+            v += f * s.F11[i + 1]
+        return v
+
+    got, exp, _, _ = _first_order(M, O, mie5, 0.7, math.radians(150.0), P11)
+    assert np.max(np.abs(got - exp) / exp) < 1e-6
+
+
+def test_cb_single_scattering_at_exact_backscatter(M, O):
+    """At order 1 the CB bin theta_b = 0 collects P11(pi) exp(-tau_a) (src/gpu.jl:142-174);
+    averaged over the first-collision depth this is omega 1.5 (1 - exp(-2 tau)) / 2."""
+    ray = M.RayleighScatterer(0.9, 1.0)
+    g = _plane(M, ray, 1.0)
+    n = 1 << 15
+    cfg = _small_cfg(M, g, n, maximum_scattering_times=1)
+    r = O.simulate(cfg, g, N0, seed=3, rng_mode=1)
+    exp = 0.9 * 1.5 * (1 - math.exp(-2.0)) / 2
+    assert abs(r["Icb"][0, 0, 0] / n / exp - 1) < 1e-6
+    assert np.allclose(r["Icb"][0, 0, :], r["Icb"][0, 0, 0], rtol=1e-12)
+
+
+def test_reciprocal_path_doubles_the_exact_backscatter_of_a_symmetric_path(M, O):
+    """For order >= 2 the coherent sum at theta_b = 0 is the ladder plus interference;
+    with Rayleigh scatterers the CB enhancement at exact backscatter is above 1 and at
+    most 2."""
+    ray = M.RayleighScatterer(1.0, 100.0)
+    g = _plane(M, ray, 3.0)
+    cfg = _small_cfg(M, g, 400, maximum_scattering_times=200)
+    r = O.simulate(cfg, g, N0, seed=9, threads=4)
+    enh = r["Icb"][0, 0, 0] / r["ladder"][0, 0]
+    assert 1.0 < enh <= 2.0
