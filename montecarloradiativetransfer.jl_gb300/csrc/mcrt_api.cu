@@ -87,6 +87,8 @@ struct mcrt_scatterer {
     d.ntheta = ntheta;
     d.rp = rp;
     d.kl = kl;
+    d.scaled = ntheta > 1 ? (ntheta - 1) / host::PI : 0.0;
+    d.scalef = (float)d.scaled;
     d.F = F.as<const float4>();
     d.S = S.as<const float4>();
     d.csrn = C.as<const float>();
@@ -552,7 +554,7 @@ int size_launch(mcrt_ctx* ctx, Group& G, const mcrt_run_opts* o, const std::stri
   if (!bs) bs = L.precision == MCRT_FP32 ? 256 : 128;
   KInfo ki;
   if (!kernel_info(L.precision, bs, ki))
-    return set_err(MCRT_EINVAL, "unsupported block size for this precision (FP32: 128/256/512, FP64: 128/256)");
+    return set_err(MCRT_EINVAL, "unsupported block size for this precision (FP32: 128/256/512/768, FP64: 128/256)");
   int tf4 = 0;
   for (auto& D : G.hinst) tf4 = std::max(tf4, table_f4_of(D));
   size_t smem = ki.shared_static + (size_t)tf4 * 16;

@@ -37,12 +37,21 @@ struct DevScatterer {
   int kind;        // 0 Rayleigh, 1 Mie
   int ntheta;      // Mie table length (the device tables carry one zero pad entry)
   int rp;          // Mie random_points
-  int pad;
+  float scalef;    // (ntheta - 1) / pi, the table index per radian, in each precision
   double kl;
   const float4* F; // (F11, F12, F33, F34) per angle, ntheta + 1
   const float4* S; // (S11re, S11im, S22re, S22im) per angle, ntheta + 1
   const float* csrn; // rp + 1 (+1 pad)
+  double scaled;
+  double pad;
 };
+
+template <typename T>
+__host__ __device__ __forceinline__ T table_scale(const DevScatterer& s);
+template <>
+__host__ __device__ __forceinline__ float table_scale<float>(const DevScatterer& s) { return s.scalef; }
+template <>
+__host__ __device__ __forceinline__ double table_scale<double>(const DevScatterer& s) { return s.scaled; }
 
 struct DevLayer {
   double tau, omega;
@@ -148,19 +157,52 @@ __device__ __forceinline__ Draw draw(unsigned k0, unsigned k1, unsigned long lon
 // ------------------------------------------------------------------ math traits
 template <typename T>
 struct MT;
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// arccos from Hastings' approximation, Abramowitz & Stegun (1964) formula 4.4.46:
+// acos(x) = sqrt(1 - x) (a0 + a1 x + ... + a7 x^7) + e(x), |e| <= 2e-8 for 0 <= x <= 1,
+// and acos(-x) = pi - acos(x).
+__device__ __forceinline__ float acos_as4446(float x) {
+  const float ax = fabsf(x);
+  float p = -0.0012624911f;
+  p = p * ax + 0.0066700901f;
+  p = p * ax - 0.0170881256f;
+  p = p * ax + 0.0308918810f;
+  p = p * ax - 0.0501743046f;
+  p = p * ax + 0.0889789874f;
+  p = p * ax - 0.2145988016f;
+  p = p * ax + 1.5707963050f;
+  const float y = fmaxf(1.0f - ax, 0.0f);
+  const float r = y > 0.0f ? y * rsqrt_approx(y) * p : 0.0f;
+  return x < 0.0f ? 3.14159265358979f - r : r;
+}
+
+// FP32 transport uses the hardware approximations (MUFU) in the hot loops; their
+// errors (about 2^-22 relative for rsqrt and exp2, 2^-20.5 absolute for sin and cos on
+// [-pi, pi]) sit far below the 1e-4 agreement required of FP32 against FP64.
 template <>
 struct MT<float> {
-  static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
+  static __device__ __forceinline__ float rsqrt(float x) { return rsqrt_approx(x); }
   static __device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
-  static __device__ __forceinline__ float exp2n(float x) { return exp2f(-x); }  // exp2(-x)
+  static __device__ __forceinline__ float exp2n(float x) {  // exp2(-x)
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(-x));
+    return r;
+  }
   static __device__ __forceinline__ float log(float x) { return logf(x); }
   static __device__ __forceinline__ float exp(float x) { return expf(x); }
-  static __device__ __forceinline__ float acos(float x) { return acosf(x); }
+  static __device__ __forceinline__ float acos(float x) { return acos_as4446(x); }
   static __device__ __forceinline__ float cbrt(float x) { return cbrtf(x); }
   static __device__ __forceinline__ void sincos(float x, float* s, float* c) { sincosf(x, s, c); }
-  static __device__ __forceinline__ void sincospi(float x, float* s, float* c) {
-    sincospif(x, s, c);
+  // sin and cos of 2 pi t for a phase t in turns with |t| <= 1/2
+  static __device__ __forceinline__ void sincos_turns(float t, float* s, float* c) {
+    __sincosf(6.28318530717958647692f * t, s, c);
   }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
   static __device__ __forceinline__ float rint(float x) { return rintf(x); }
   static __device__ __forceinline__ float floor(float x) { return floorf(x); }
   static __device__ __forceinline__ float fabs(float x) { return fabsf(x); }
@@ -181,6 +223,10 @@ struct MT<double> {
   static __device__ __forceinline__ void sincospi(double x, double* s, double* c) {
     ::sincospi(x, s, c);
   }
+  static __device__ __forceinline__ void sincos_turns(double t, double* s, double* c) {
+    ::sincospi(2.0 * t, s, c);
+  }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
   static __device__ __forceinline__ double rint(double x) { return ::rint(x); }
   static __device__ __forceinline__ double floor(double x) { return ::floor(x); }
   static __device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
@@ -259,13 +305,13 @@ struct PMat {
 // phase_matrix evaluated at a given cosine (src/scatterers/rayleigh.jl:13-16,
 // src/scatterers/mie.jl:53-71); Mie reads the padded FP32 table F.
 template <typename T>
-__device__ __forceinline__ PMat<T> phase_eval(int kind, const float4* F, int ntheta, T mu) {
+__device__ __forceinline__ PMat<T> phase_eval(int kind, const float4* F, int ntheta, T scale, T mu) {
   if (kind == 0) {
     T m2 = mu * mu;
     return PMat<T>{T(0.75) + T(0.75) * m2, T(-0.75) + T(0.75) * m2, T(1.5) * mu, T(0)};
   }
   T th = MT<T>::acos(clamp1(mu));
-  T sn = th * (T)((ntheta - 1) / PI_D);
+  T sn = th * scale;
   int i0 = (int)sn;
   i0 = i0 > ntheta - 1 ? ntheta - 1 : i0;
   T f = sn - (T)i0;
@@ -279,7 +325,7 @@ __device__ __forceinline__ PMat<T> phase_eval(int kind, const float4* F, int nth
 // amplitude_matrix diagonal (src/scatterers/rayleigh.jl:20-23, src/scatterers/mie.jl:76-92,
 // keeping the reference's (2 - f, f - 1) interpolation weights of mie.jl:80-85).
 template <typename T>
-__device__ __forceinline__ void amp_eval(int kind, const float4* S, int ntheta, T mu, T& s1r,
+__device__ __forceinline__ void amp_eval(int kind, const float4* S, int ntheta, T scale, T mu, T& s1r,
                                          T& s1i, T& s2r, T& s2i) {
   if (kind == 0) {
     s1r = T(0);
@@ -289,7 +335,7 @@ __device__ __forceinline__ void amp_eval(int kind, const float4* S, int ntheta, 
     return;
   }
   T th = MT<T>::acos(clamp1(mu));
-  T sn = th * (T)((ntheta - 1) / PI_D);
+  T sn = th * scale;
   int i0 = (int)sn;
   i0 = i0 > ntheta - 1 ? ntheta - 1 : i0;
   T f = sn - (T)i0;
@@ -374,13 +420,14 @@ __device__ __forceinline__ void psi_angles(const Frame<T>& f, const Frame<T>& ks
 // update_I (src/utils.jl:91-112) for a general outgoing direction k with basis Eh.
 template <typename T>
 __device__ __forceinline__ void update_I(const Frame<T>& f, const T I[4], T kx, T ky, T kz, T ehx,
-                                         T ehy, int kind, const float4* F, int ntheta, T out[4]) {
+                                         T ehy, int kind, const float4* F, int ntheta, T scale,
+                                         T out[4]) {
   T rx, ry, rz;
   norm_to_ray(f, kx, ky, kz, rx, ry, rz);
   Frame<T> ks = spherical(rx, ry, rz);
   T cpsi, spsi;
   psi_angles(f, ks, ehx, ehy, T(-1), cpsi, spsi);
-  PMat<T> P = phase_eval<T>(kind, F, ntheta, rz);
+  PMat<T> P = phase_eval<T>(kind, F, ntheta, scale, rz);
   T q = I[1], u = I[2];
   rotate(ks.cp * ks.cp - ks.sp * ks.sp, T(-2) * ks.sp * ks.cp, q, u);
   out[0] = P.p11 * I[0] + P.p12 * q;
@@ -393,14 +440,14 @@ __device__ __forceinline__ void update_I(const Frame<T>& f, const T I[4], T kx, 
 // update_E (src/utils.jl:170-192) on E = (E1re, E1im, E2re, E2im), in place.
 template <typename T>
 __device__ __forceinline__ void update_E(const Frame<T>& f, T E[4], T kx, T ky, T kz, T ehx, T ehy,
-                                         int kind, const float4* S, int ntheta) {
+                                         int kind, const float4* S, int ntheta, T scale) {
   T rx, ry, rz;
   norm_to_ray(f, kx, ky, kz, rx, ry, rz);
   Frame<T> ks = spherical(rx, ry, rz);
   T cpsi, spsi;
   psi_angles(f, ks, ehx, ehy, T(1), cpsi, spsi);
   T s1r, s1i, s2r, s2i;
-  amp_eval<T>(kind, S, ntheta, rz, s1r, s1i, s2r, s2i);
+  amp_eval<T>(kind, S, ntheta, scale, rz, s1r, s1i, s2r, s2i);
   T ar = E[0] * ks.cp + E[2] * ks.sp, ai = E[1] * ks.cp + E[3] * ks.sp;
   T br = -E[0] * ks.sp + E[2] * ks.cp, bi = -E[1] * ks.sp + E[3] * ks.cp;
   T sar = s1r * ar - s1i * ai, sai = s1r * ai + s1i * ar;
@@ -415,7 +462,7 @@ __device__ __forceinline__ void update_E(const Frame<T>& f, T E[4], T kx, T ky, 
 // Stored as m[8] = (m11r, m11i, m12r, m12i, m21r, m21i, m22r, m22i).
 template <typename T>
 __device__ __forceinline__ void update_E_matrix(const Frame<T>& f, T kx, T ky, T kz, int kind,
-                                                const float4* S, int ntheta, T m[8]) {
+                                                const float4* S, int ntheta, T scale, T m[8]) {
   T ehx, ehy;
   basis_h(kx, ky, ehx, ehy);
   T rx, ry, rz;
@@ -424,7 +471,7 @@ __device__ __forceinline__ void update_E_matrix(const Frame<T>& f, T kx, T ky, T
   T cpsi, spsi;
   psi_angles(f, ks, ehx, ehy, T(1), cpsi, spsi);
   T s1r, s1i, s2r, s2i;
-  amp_eval<T>(kind, S, ntheta, rz, s1r, s1i, s2r, s2i);
+  amp_eval<T>(kind, S, ntheta, scale, rz, s1r, s1i, s2r, s2i);
   T c = ks.cp, s = ks.sp;
   // M11 = cpsi S11 c - spsi S22 s ; M12 = cpsi S11 s + spsi S22 c
   // M21 = -spsi S11 c - cpsi S22 s ; M22 = -spsi S11 s + cpsi S22 c

@@ -19,6 +19,10 @@ bool kernel_info_fp32(int bs, KInfo& k) {
       k.fn = k_transport<float, 512, 4, 2, 1>;
       k.shared_static = sizeof(Shared<float, 512>);
       return true;
+    case 768:  // one block per SM with 24 warps, at most 85 registers per thread
+      k.fn = k_transport<float, 768, 4, 2, 1>;
+      k.shared_static = sizeof(Shared<float, 768>);
+      return true;
   }
   return false;
 }

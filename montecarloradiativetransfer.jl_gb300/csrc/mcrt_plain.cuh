@@ -85,7 +85,7 @@ __device__ __forceinline__ void plain_update_I(const DevScatterer& s, const T I[
                                                const Frame<T>& f, T out[4]) {
   PV3<T> Eh, Ev;
   plain_basis(k, Eh, Ev);
-  update_I<T>(f, I, k.x, k.y, k.z, Eh.x, Eh.y, s.kind, s.F, s.ntheta, out);
+  update_I<T>(f, I, k.x, k.y, k.z, Eh.x, Eh.y, s.kind, s.F, s.ntheta, table_scale<T>(s), out);
 }
 
 template <typename T>
@@ -93,7 +93,7 @@ __device__ __forceinline__ void plain_update_E(const DevScatterer& s, T E[4], PV
                                                const Frame<T>& f) {
   PV3<T> Eh, Ev;
   plain_basis(k, Eh, Ev);
-  update_E<T>(f, E, k.x, k.y, k.z, Eh.x, Eh.y, s.kind, s.S, s.ntheta);
+  update_E<T>(f, E, k.x, k.y, k.z, Eh.x, Eh.y, s.kind, s.S, s.ntheta, table_scale<T>(s));
 }
 
 template <typename T>
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(256) k_plain(PlainParams p) {
         } else {
           mu = sample_mu<T>(1, sc.csrn, sc.rp, u0);
         }
-        PMat<T> P = phase_eval<T>(sc.kind, sc.F, sc.ntheta, mu);
+        PMat<T> P = phase_eval<T>(sc.kind, sc.F, sc.ntheta, table_scale<T>(sc), mu);
         T eq = -P.p12 * I[1] / (P.p11 * I[0]), eu = -P.p12 * I[2] / (P.p11 * I[0]);
         T ee = MT<T>::sqrt(eq * eq + eu * eu);
         T phi;

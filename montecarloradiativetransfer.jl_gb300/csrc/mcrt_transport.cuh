@@ -121,7 +121,7 @@ __device__ __forceinline__ T warp_sum(T v) {
 template <typename T>
 __device__ __forceinline__ T sphere_t(T kx, T D) {
   T r = MT<T>::sqrt(kx * kx + D);
-  return kx > T(0) ? D / (kx + r) : r - kx;
+  return kx > T(0) ? MT<T>::div(D, kx + r) : r - kx;
 }
 
 // ------------------------------------------------------------------ instance staging
@@ -300,7 +300,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
       }
       Frame<T> fr = n == 2 ? inc : spherical(ps.kprev[0], ps.kprev[1], ps.kprev[2]);
       T m[8], a[4];
-      update_E_matrix(fr, ps.k[0], ps.k[1], ps.k[2], s1.kind, s1.S, s1.ntheta, m);
+      update_E_matrix(fr, ps.k[0], ps.k[1], ps.k[2], s1.kind, s1.S, s1.ntheta, table_scale<T>(s1), m);
       mat2_vec(m, ps.A, a);
       T na = MT<T>::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3]);
       T ina = T(1) / na;
@@ -308,7 +308,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
       ps.logA += log((double)na);
       if (n >= 3) {
         Frame<T> fm = spherical(-ps.k[0], -ps.k[1], -ps.k[2]);
-        update_E_matrix(fm, -ps.kprev[0], -ps.kprev[1], -ps.kprev[2], s1.kind, s1.S, s1.ntheta, m);
+        update_E_matrix(fm, -ps.kprev[0], -ps.kprev[1], -ps.kprev[2], s1.kind, s1.S, s1.ntheta, table_scale<T>(s1), m);
         mat2_mul(ps.L, m, ps.L);
         T nl = T(0);
         for (int s = 0; s < 8; ++s) nl += ps.L[s] * ps.L[s];
@@ -345,7 +345,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
     T u0 = u01<T>(d.r[0]), u1 = u01<T>(d.r[1]), u2 = u01<T>(d.r[2]);
     // scatter (src/utils.jl:294-323)
     T mu = sample_mu<T>(sc.kind, sc.csrn, sc.rp, u0);
-    PMat<T> P = phase_eval<T>(sc.kind, sc.F, sc.ntheta, mu);
+    PMat<T> P = phase_eval<T>(sc.kind, sc.F, sc.ntheta, table_scale<T>(sc), mu);
     T den = P.p11 * I[0];
     T eq = -P.p12 * I[1] / den, eu = -P.p12 * I[2] / den;
     T ee = MT<T>::sqrt(eq * eq + eu * eu);
@@ -461,15 +461,15 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
     ev.bsp = kbs.sp;
     T m[8], Ei[4], tmp[4], b[4];
     for (int s = 0; s < 4; ++s) Ei[s] = (T)in.Ei[s];
-    update_E_matrix(inc, -ps.k[0], -ps.k[1], -ps.k[2], s1.kind, s1.S, s1.ntheta, m);
+    update_E_matrix(inc, -ps.k[0], -ps.k[1], -ps.k[2], s1.kind, s1.S, s1.ntheta, table_scale<T>(s1), m);
     mat2_vec(m, Ei, tmp);
     mat2_vec(ps.L, tmp, b);
     const T kf0x = (T)in.kf0[0], kf0y = (T)in.kf0[1], kf0z = (T)in.kf0[2];
     const T eh0x = (T)in.eh0[0], eh0y = (T)in.eh0[1];
     T Iaf0[4];
-    update_I(ks, Ia, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.F, s1.ntheta, Iaf0);
+    update_I(ks, Ia, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.F, s1.ntheta, table_scale<T>(s1), Iaf0);
     T Ef[4] = {ps.A[0], ps.A[1], ps.A[2], ps.A[3]};
-    update_E(ks, Ef, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.S, s1.ntheta);
+    update_E(ks, Ef, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.S, s1.ntheta, table_scale<T>(s1));
     T nf = Ef[0] * Ef[0] + Ef[1] * Ef[1] + Ef[2] * Ef[2] + Ef[3] * Ef[3];
     T c = MT<T>::sqrt(Iaf0[0] / nf);
     T rb = (T)exp(ps.logL - ps.logA) * c;
@@ -531,7 +531,7 @@ struct RTLane {
 
 template <typename T, int NB, bool MIE, bool SPHERE>
 __device__ __forceinline__ T rt_event(RTLane<T, NB>& R, const EventP<T>& E, const float4* F,
-                                      int ntheta, T tau0l, bool upper) {
+                                      int ntheta, T scale, T tau0l, bool upper) {
   const T fct = E.fct, fst = E.fst, fcp = E.fcp, fsp = E.fsp;
   const T sD = R.sb * fcp - R.cb * fsp, cD = R.cb * fcp + R.sb * fsp;
   const T a1 = fct * cD, a3 = fst * cD, bq = fct * sD, c4 = fst * sD;
@@ -570,7 +570,7 @@ __device__ __forceinline__ T rt_event(RTLane<T, NB>& R, const EventP<T>& E, cons
     const T c2p = cpsi * cpsi - spsi * spsi, s2p = T(2) * spsi * cpsi;
     PMat<T> P;
     if (MIE) {
-      P = phase_eval<T>(1, F, ntheta, k3);
+      P = phase_eval<T>(1, F, ntheta, scale, k3);
     } else {
       const T m2 = k3 * k3;
       P = PMat<T>{T(0.75) + T(0.75) * m2, T(-0.75) + T(0.75) * m2, T(1.5) * k3, T(0)};
@@ -598,7 +598,8 @@ __device__ __forceinline__ T rt_event(RTLane<T, NB>& R, const EventP<T>& E, cons
 }
 
 template <typename T, int NB, int BS>
-__device__ void rt_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool upper, int pc) {
+__device__ void rt_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool upper, int pc, int q0,
+                        int q1) {
   const int lane = threadIdx.x & 31;
   const int r0 = upper ? B.up0 : B.lo0, r1 = upper ? B.up1 : B.lo1;
   const int ngrp = (r1 - r0 + NB - 1) / NB;
@@ -624,20 +625,20 @@ __device__ void rt_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool
   const DevInstance& in = sh.inst;
   const T tau0l = (T)(in.tau0 * LOG2E_D);
   const int li = upper ? 0 : 1;
-  const int ne = sh.cnt[pc][li];
   T* escarr = upper ? sh.esc_up : sh.esc_dn;
   const bool sphere = in.geom == 1;
-  for (int q = 0; q < ne; ++q) {
+  for (int q = q0; q < q1; ++q) {
     const int e = sh.list[li][q];
     const EventP<T>& E = sh.ev[e];
     const DevScatterer& sc = in.scat[E.layer];
     T esc;
     if (sc.kind == 1) {
-      esc = sphere ? rt_event<T, NB, true, true>(R, E, sc.F, sc.ntheta, tau0l, upper)
-                   : rt_event<T, NB, true, false>(R, E, sc.F, sc.ntheta, tau0l, upper);
+      const T scale = table_scale<T>(sc);
+      esc = sphere ? rt_event<T, NB, true, true>(R, E, sc.F, sc.ntheta, scale, tau0l, upper)
+                   : rt_event<T, NB, true, false>(R, E, sc.F, sc.ntheta, scale, tau0l, upper);
     } else {
-      esc = sphere ? rt_event<T, NB, false, true>(R, E, sc.F, sc.ntheta, tau0l, upper)
-                   : rt_event<T, NB, false, false>(R, E, sc.F, sc.ntheta, tau0l, upper);
+      esc = sphere ? rt_event<T, NB, false, true>(R, E, sc.F, sc.ntheta, T(0), tau0l, upper)
+                   : rt_event<T, NB, false, false>(R, E, sc.F, sc.ntheta, T(0), tau0l, upper);
     }
     esc = warp_sum(esc);
     if (lane == 0) atomicAdd(&escarr[e], esc);
@@ -669,18 +670,19 @@ __device__ __forceinline__ T cbn_event(CBLane<T, NB>& C, const EventP<T>& E, con
                                        T tau0l, bool peak_lane) {
   const Frame<T> fa{E.fct, E.fst, E.fcp, E.fsp};
   const Frame<T> fb{E.bct, E.bst, E.bcp, E.bsp};
+  const T scale = table_scale<T>(s1);
   T pk = T(0);
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     T ea[4] = {E.ea[0], E.ea[1], E.ea[2], E.ea[3]};
     T eb[4] = {E.eb[0], E.eb[1], E.eb[2], E.eb[3]};
-    update_E<T>(fa, ea, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.S, s1.ntheta);
-    update_E<T>(fb, eb, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.S, s1.ntheta);
+    update_E<T>(fa, ea, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.S, s1.ntheta, scale);
+    update_E<T>(fb, eb, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.S, s1.ntheta, scale);
     // Phase kl (ki + kf).(xa - xb) in turns, cancellation-free in the backscatter frame.
     const T turns = C.c1[i] * E.v1 + C.c2[i] * E.v2 + C.c3[i] * E.v3;
     const T fr = turns - MT<T>::rint(turns);
     T sn, cs;
-    MT<T>::sincospi(T(2) * fr, &sn, &cs);
+    MT<T>::sincos_turns(fr, &sn, &cs);
     T ta2, tb2;
     if (SPHERE) {
       ta2 = sphere_t(C.kx[i] * E.xax + C.ky[i] * E.xay + C.kz[i] * E.xaz, E.Da) * T(LOG2E_D);
@@ -707,7 +709,7 @@ __device__ __forceinline__ T cbn_event(CBLane<T, NB>& C, const EventP<T>& E, con
     T S2 = T(2) * (c2r * c1r + c2i * c1i), S3 = T(-2) * (c2i * c1r - c2r * c1i);
     const T den = Ia + Ib;
     const bool ok = ma && den > T(0);
-    const T scl = ok ? Ia / den : T(0);
+    const T scl = ok ? MT<T>::div(Ia, den) : T(0);
     S0 *= scl;
     S1 *= scl;
     S2 *= scl;
@@ -727,12 +729,13 @@ template <typename T, int NB, bool MIE, bool SPHERE>
 __device__ __forceinline__ T cb1_event(CBLane<T, NB>& C, const EventP<T>& E, const DevScatterer& s1,
                                        T tau0l, bool peak_lane) {
   const Frame<T> fa{E.fct, E.fst, E.fcp, E.fsp};
+  const T scale = table_scale<T>(s1);
   T pk = T(0);
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     T o[4];
     update_I<T>(fa, E.I, C.kx[i], C.ky[i], C.kz[i], C.ehx[i], C.ehy[i], MIE ? 1 : 0, s1.F, s1.ntheta,
-                o);
+                scale, o);
     T ta2;
     if (SPHERE)
       ta2 = sphere_t(C.kx[i] * E.xax + C.ky[i] * E.xay + C.kz[i] * E.xaz, E.Da) * T(LOG2E_D);
@@ -752,7 +755,7 @@ __device__ __forceinline__ T cb1_event(CBLane<T, NB>& C, const EventP<T>& E, con
 }
 
 template <typename T, int NB, int BS>
-__device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int pc) {
+__device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int pc, int q0, int q1) {
   const int lane = threadIdx.x & 31;
   const int ngrp = (B.nthetab + NB - 1) / NB;
   const int item = tile * 32 + lane;
@@ -786,8 +789,9 @@ __device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int 
   const DevScatterer& s1 = in.scat[in.layers[0].scat];
   const T tau0l = (T)(in.tau0 * LOG2E_D);
   const bool sphere = in.geom == 1, mie = s1.kind == 1;
+  // events [q0, q1) of the concatenated lists (order > 1, then order 1)
   const int nn = sh.cnt[pc][2];
-  for (int q = 0; q < nn; ++q) {
+  for (int q = q0; q < min(q1, nn); ++q) {
     const int e = sh.list[2][q];
     const EventP<T>& E = sh.ev[e];
     T pk;
@@ -799,9 +803,8 @@ __device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int 
                   : cbn_event<T, NB, false, false>(C, E, s1, tau0l, peak_lane);
     if (peak_lane) sh.peak[e] = pk;
   }
-  const int n1 = sh.cnt[pc][3];
-  for (int q = 0; q < n1; ++q) {
-    const int e = sh.list[3][q];
+  for (int q = max(q0, nn); q < q1; ++q) {
+    const int e = sh.list[3][q - nn];
     const EventP<T>& E = sh.ev[e];
     T pk;
     if (mie)
@@ -930,7 +933,13 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
       const int tcb = nc ? (B.nphib * ((B.nthetab + NBC - 1) / NBC) + 31) / 32 : 0;
       const int tup = nu ? (B.nphi * ((B.up1 - B.up0 + NBR - 1) / NBR) + 31) / 32 : 0;
       const int tdn = nd ? (B.nphi * ((B.lo1 - B.lo0 + NBR - 1) / NBR) + 31) / 32 : 0;
-      const int total = tcb + tup + tdn;
+      // Work items are (tile, chunk of up to EVC events); the costlier CB items go first.
+      // Chunks only split batches larger than 256 events: below that, the extra tally
+      // flushes cost more than the better balance gains.
+      constexpr int EVC = 256;
+      const int ccb = (nc + EVC - 1) / EVC, cup = (nu + EVC - 1) / EVC, cdn = (nd + EVC - 1) / EVC;
+      const int icb = tcb * ccb, iup = tup * cup, idn = tdn * cdn;
+      const int total = icb + iup + idn;
       if (tid == 0)
         for (int l = 0; l < 4; ++l) sh.cnt[pc ^ 1][l] = 0;
       for (;;) {
@@ -938,12 +947,18 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
         if (lane == 0) w = atomicAdd(&sh.item_next, 1);
         w = __shfl_sync(0xffffffffu, w, 0);
         if (w >= total) break;
-        if (w < tcb)
-          cb_tile<T, NBC, BS>(sh, B, w, pc);
-        else if (w < tcb + tup)
-          rt_tile<T, NBR, BS>(sh, B, w - tcb, true, pc);
-        else
-          rt_tile<T, NBR, BS>(sh, B, w - tcb - tup, false, pc);
+        if (w < icb) {
+          const int c = w % ccb;
+          cb_tile<T, NBC, BS>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
+        } else if (w < icb + iup) {
+          w -= icb;
+          const int c = w % cup;
+          rt_tile<T, NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
+        } else {
+          w -= icb + iup;
+          const int c = w % cdn;
+          rt_tile<T, NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
+        }
       }
     }
     __syncthreads();
