@@ -214,6 +214,34 @@ int mcrt_batch_read(mcrt_batch* b, int i, double A_out[5], double* Irt, double* 
 int mcrt_batch_timing(mcrt_batch* b, double* kernel_ms, double* photons);
 int mcrt_batch_destroy(mcrt_batch* b);
 
+/* ------------------------------------------------------------------ no device allocation */
+/* Size of the device array that mcrt_simulate_noalloc works in (24 MiB). */
+#define MCRT_NOALLOC_SCRATCH_BYTES (24u << 20)
+
+/* mcrt_simulate without device allocation. No counterpart in the reference.
+ *
+ * Same arguments, outputs and results as mcrt_simulate on the persistent kernel, for
+ * callers that must not allocate device memory when they call: for example a host
+ * application whose device memory is entirely reserved by its own allocator at start
+ * up, or a loop that is not allowed to allocate once it runs. It calls no cudaMalloc,
+ * cudaFree or other device allocator. Everything the call needs on the device besides
+ * the caller's scatterers (created beforehand with mcrt_scatterer_create) lives in one
+ * file-scope device array of MCRT_NOALLOC_SCRATCH_BYTES bytes, which every GPU that
+ * loads the library holds until the process exits: the instance descriptor, the bin
+ * tables, the tallies, the work counters and the photon-state pool. It runs one block
+ * per SM, so it is slower than mcrt_simulate.
+ *
+ * - A config whose bin tables and tallies do not fit in the array beside the
+ *   photon-state pool is rejected with MCRT_EINVAL and a message giving both sizes.
+ * - The first call on a device looks up the array's device address; make that first
+ *   call before any stream capture on that device.
+ * - Every call reuses the same array: each call clears the tallies and counters it
+ *   needs before its launch, and calls that overlap on the GPU (from several threads or
+ *   contexts on one device) race on the array and must be serialised by the caller. */
+int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g,
+                          const double I0[4], const mcrt_run_opts* opts, double A_out[5],
+                          double* Irt, double* Icb, double* Icb_ladder, mcrt_stats* stats);
+
 /* ------------------------------------------------------------------ measurement */
 /* Measured FP32 FMA throughput of this device (TFLOP/s, FMA = 2 flops) from a short
  * dependent-FMA microbenchmark; used as the roofline peak of the transport kernel. */

@@ -931,3 +931,213 @@ extern "C" int mcrt_measure_fp32_peak(mcrt_ctx* ctx, double* tflops) {
   *tflops = flops / (best * 1e-3) / 1e12;
   return MCRT_OK;
 }
+
+// ================================================================== no device allocation
+// mcrt_simulate_noalloc: the persistent-kernel simulate for callers that must not
+// allocate device memory at call time (declared in include/mcrt.h, which states the
+// contract). All call-time device storage lives in g_noalloc_scratch below.
+namespace {
+
+// The device array every mcrt_simulate_noalloc call works in. Each GPU that loads the
+// library holds it until the process exits; calls reuse it, so overlapping calls race.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MCRT_NOALLOC_SCRATCH_BYTES];
+
+// In host code g_noalloc_scratch names a host-side stand-in, not a device address, so
+// the device address is looked up once per device (with that device current) and kept.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_base[NOALLOC_MAX_DEVICES] = {};
+
+int noalloc_base(int device, unsigned char** out) {
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+    return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc: device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_base[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return set_err(MCRT_ECUDA, std::string("mcrt_simulate_noalloc: cudaGetSymbolAddress failed: ") +
+                                     cudaGetErrorString(e));
+    g_noalloc_base[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_base[device];
+  return MCRT_OK;
+}
+
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+// The bin tables of upload_bins laid out at a given device address, as host bytes.
+template <typename T>
+std::vector<unsigned char> pack_bins_at(const HostBins& H, const unsigned char* dev) {
+  Packer P;
+  BinTables<T> hdr{};
+  P.add(&hdr, sizeof(hdr));
+  auto addv = [&](const std::vector<double>& v) {
+    std::vector<T> t(v.begin(), v.end());
+    if (t.empty()) t.push_back(T(0));
+    return P.add(t.data(), t.size() * sizeof(T));
+  };
+  size_t o_st = addv(H.st), o_ct = addv(H.ct), o_g = addv(H.g), o_w = addv(H.w), o_cp = addv(H.cp),
+         o_sp = addv(H.sp);
+  size_t o_kfx = addv(H.kfx), o_kfy = addv(H.kfy), o_kfz = addv(H.kfz), o_ehx = addv(H.ehx),
+         o_ehy = addv(H.ehy), o_gb = addv(H.gb), o_cf2 = addv(H.cf2), o_sf2 = addv(H.sf2),
+         o_c1 = addv(H.c1), o_c2 = addv(H.c2), o_c3 = addv(H.c3);
+  size_t o_upb = P.add(H.upb.data(), H.upb.size() * sizeof(int));
+  size_t o_stb = addv(H.stb), o_ctb = addv(H.ctb), o_cpb = addv(H.cpb), o_spb = addv(H.spb);
+  hdr.ntheta = H.ntheta;
+  hdr.nphi = H.nphi;
+  hdr.nthetab = H.nthetab;
+  hdr.nphib = H.nphib;
+  hdr.up0 = H.up0;
+  hdr.up1 = H.up1;
+  hdr.lo0 = H.lo0;
+  hdr.lo1 = H.lo1;
+  auto at = [&](size_t o) { return reinterpret_cast<const T*>(dev + o); };
+  hdr.st = at(o_st);
+  hdr.ct = at(o_ct);
+  hdr.g = at(o_g);
+  hdr.w = at(o_w);
+  hdr.cp = at(o_cp);
+  hdr.sp = at(o_sp);
+  hdr.kfx = at(o_kfx);
+  hdr.kfy = at(o_kfy);
+  hdr.kfz = at(o_kfz);
+  hdr.ehx = at(o_ehx);
+  hdr.ehy = at(o_ehy);
+  hdr.gb = at(o_gb);
+  hdr.cf2 = at(o_cf2);
+  hdr.sf2 = at(o_sf2);
+  hdr.c1 = at(o_c1);
+  hdr.c2 = at(o_c2);
+  hdr.c3 = at(o_c3);
+  hdr.upb = reinterpret_cast<const int*>(dev + o_upb);
+  hdr.stb = at(o_stb);
+  hdr.ctb = at(o_ctb);
+  hdr.cpb = at(o_cpb);
+  hdr.spb = at(o_spb);
+  std::memcpy(P.bytes.data(), &hdr, sizeof(hdr));
+  return P.bytes;
+}
+
+}  // namespace
+
+extern "C" int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g,
+                                     const double I0[4], const mcrt_run_opts* opts, double A_out[5],
+                                     double* Irt, double* Icb, double* Icb_ladder, mcrt_stats* stats) {
+  if (!ctx || !I0 || !A_out || !Irt || !Icb)
+    return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc: NULL argument");
+  int rc = validate_geometry(g);
+  if (rc) return rc;
+  rc = validate_config(cfg, g->kind);
+  if (rc) return rc;
+  const int prec = opts ? opts->precision : MCRT_FP32;
+  if (prec != MCRT_FP32 && prec != MCRT_FP64)
+    return set_err(MCRT_EINVAL, "precision must be MCRT_FP32 or MCRT_FP64");
+  if (opts && opts->kernel != MCRT_KERNEL_PERSISTENT)
+    return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc runs the persistent kernel only");
+  CK(cudaSetDevice(ctx->device));
+  unsigned char* base = nullptr;
+  rc = noalloc_base(ctx->device, &base);
+  if (rc) return rc;
+
+  DevInstance D;
+  host::Sph kfs;
+  rc = make_instance(cfg, g, I0, opts ? opts->seed : 0, opts ? opts->instance : 0, opts ? opts->rng_mode : 0,
+                     cfg->number_of_rays, opts ? opts->photon_begin : 0, D, kfs);
+  if (rc) return rc;
+  HostBins H = make_bins(cfg, g->kind, kfs);
+
+  // Launch shape: one block per SM.
+  const int bs = prec == MCRT_FP32 ? 256 : 128;
+  KInfo ki;
+  if (!kernel_info(prec, bs, ki)) return set_err(MCRT_EINVAL, "no kernel for this precision");
+  int tf4 = table_f4_of(D);
+  size_t smem = ki.shared_static + (size_t)tf4 * 16;
+  if (smem > (size_t)ctx->smem_optin) {
+    tf4 = (int)((ctx->smem_optin - ki.shared_static) / 16);
+    smem = ki.shared_static + (size_t)tf4 * 16;
+  }
+  CK(cudaFuncSetAttribute(ki.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = ctx->sms;
+  const size_t slots = (size_t)blocks * bs;
+
+  // Layout of the scratch array.
+  const size_t nrt = 4 * (size_t)cfg->n_theta * cfg->n_phi, ncb = 4 * (size_t)cfg->n_theta_b * cfg->n_phi_b;
+  const size_t per_inst = nrt + ncb + ncb / 4 + NACC;
+  std::vector<unsigned char> binbytes;
+  const size_t off_inst = 0;
+  const size_t off_bins = align256(sizeof(DevInstance));
+  binbytes = prec == MCRT_FP32 ? pack_bins_at<float>(H, base + off_bins) : pack_bins_at<double>(H, base + off_bins);
+  const size_t off_tally = align256(off_bins + binbytes.size());
+  const size_t off_claim = align256(off_tally + per_inst * sizeof(double));
+  const size_t off_status = off_claim + sizeof(unsigned long long);
+  const size_t off_state = align256(off_status + sizeof(unsigned));
+  const size_t off_tacc = align256(off_state + slots * ki.state_bytes);
+  const size_t need = off_tacc + slots * NACC * sizeof(double);
+  if (need > MCRT_NOALLOC_SCRATCH_BYTES) {
+    char msg[256];
+    std::snprintf(msg, sizeof msg,
+                  "mcrt_simulate_noalloc: this config needs %zu bytes of device scratch; the array holds %u "
+                  "(MCRT_NOALLOC_SCRATCH_BYTES); use mcrt_simulate",
+                  need, (unsigned)MCRT_NOALLOC_SCRATCH_BYTES);
+    return set_err(MCRT_EINVAL, msg);
+  }
+  double* tally = reinterpret_cast<double*>(base + off_tally);
+  D.bins = base + off_bins;
+  D.Irt = tally;
+  D.Icb = tally + nrt;
+  D.ladder = tally + nrt + ncb;
+  D.acc = tally + nrt + ncb + ncb / 4;
+  D.claim = reinterpret_cast<unsigned long long*>(base + off_claim);
+
+  // The array keeps the previous call's contents: write the inputs and clear the
+  // tallies, the claim counter and the status word (the kernel clears its per-thread
+  // accumulators itself).
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(base + off_inst, &D, sizeof(DevInstance), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(base + off_bins, binbytes.data(), binbytes.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(base + off_tally, 0, off_state - off_tally, st));
+  KParams p;
+  p.inst = reinterpret_cast<const DevInstance*>(base + off_inst);
+  p.n_inst = 1;
+  p.state = reinterpret_cast<uint4*>(base + off_state);
+  p.tacc = reinterpret_cast<double*>(base + off_tacc);
+  p.status = reinterpret_cast<unsigned*>(base + off_status);
+  p.table_f4 = tf4;
+  CK(cudaEventRecord(ctx->e0, st));
+  CK(launch_transport(ki, blocks, bs, smem, st, p));
+  CK(cudaEventRecord(ctx->e1, st));
+  CK(cudaEventSynchronize(ctx->e1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->e0, ctx->e1));
+  std::vector<double> h(per_inst);
+  unsigned status = 0;
+  CK(cudaMemcpy(h.data(), tally, per_inst * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&status, base + off_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+
+  const double inv = cfg->number_of_rays > 0 ? 1.0 / (double)cfg->number_of_rays : 0.0;
+  const double* acc = h.data() + nrt + ncb + ncb / 4;
+  for (int s = 0; s < 5; ++s) A_out[s] = acc[s] * inv;
+  for (size_t i = 0; i < nrt; ++i) Irt[i] = h[i] * inv;
+  for (size_t i = 0; i < ncb; ++i) Icb[i] = h[nrt + i] * inv;
+  if (Icb_ladder)
+    for (size_t i = 0; i < ncb / 4; ++i) Icb_ladder[i] = h[nrt + ncb + i] * inv;
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->cb_peak_sum = acc[ACC_PEAK];
+    stats->cb_peak_sumsq = acc[ACC_PEAK2];
+    stats->photons = acc[ACC_PHOTONS];
+    stats->events = acc[ACC_EVENTS];
+    stats->attempts = acc[ACC_ATTEMPTS];
+    stats->rt_evals = acc[ACC_RT];
+    stats->cb1_evals = acc[ACC_CB1];
+    stats->cbn_evals = acc[ACC_CBN];
+    stats->kernel_ms = ms;
+    stats->status_flags = (int)status;
+    stats->block_size = bs;
+    stats->blocks = blocks;
+  }
+  if (status & MCRT_FLAG_REJECT_LIMIT)
+    return set_err(MCRT_ENONCONV, "a rejection loop hit its iteration cap; see stats.status_flags");
+  return MCRT_OK;
+}
