@@ -25,6 +25,8 @@
 // left to claim, so uneven batches run in one persistent launch.
 #pragma once
 
+#include <type_traits>
+
 #include "mcrt_device.cuh"
 
 namespace mcrt {
@@ -656,6 +658,185 @@ __device__ void rt_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool
   }
 }
 
+// ------------------------------------------------------------------ collect: RT tile, FP32x2
+// The FP32 RT peel-off with two polar bins per packed FP32x2 instruction (FFMA2, FMUL2,
+// FADD2 of sm_100 and later): same arithmetic as rt_event, half the issued FP32
+// instructions. Steps without a packed form (MUFU, conversions, table loads, selects)
+// run per bin.
+struct P2 {
+  float2 v;
+};
+__device__ __forceinline__ P2 p2(float a, float b) { return P2{make_float2(a, b)}; }
+__device__ __forceinline__ P2 p2s(float a) { return P2{make_float2(a, a)}; }
+__device__ __forceinline__ P2 operator*(P2 a, P2 b) { return P2{__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ P2 operator+(P2 a, P2 b) { return P2{__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) { return P2{__ffma2_rn(a.v, b.v, c.v)}; }
+
+template <int NP>
+struct RTLaneF2 {
+  P2 st[NP], ct[NP], g[NP], w[NP];
+  float cb, sb;
+  P2 acc[NP][4];
+};
+
+template <int NP, bool MIE, bool SPHERE>
+__device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float>& E, const float4* F,
+                                             int ntheta, float scale, float tau0l, bool upper) {
+  const float fct = E.fct, fst = E.fst, fcp = E.fcp, fsp = E.fsp;
+  const float sD = R.sb * fcp - R.cb * fsp, cD = R.cb * fcp + R.sb * fsp;
+  const P2 A1 = p2s(fct * cD), A3 = p2s(fst * cD), NFST = p2s(-fst), FCT = p2s(fct), SD = p2s(sD);
+  const P2 BQ = p2s(fct * sD), NBQ = p2s(-fct * sD), CD = p2s(cD), C4 = p2s(fst * sD);
+  const float I0 = E.I[0], I1 = E.I[1], I2 = E.I[2], I3 = E.I[3];
+  const P2 PI0 = p2s(I0), PI1 = p2s(I1), PI2 = p2s(I2), PI3 = p2s(I3);
+  const P2 M2I2 = p2s(-2.0f * I2), P2I1 = p2s(2.0f * I1), M1 = p2s(-1.0f), ONE = p2s(1.0f);
+  const P2 A = p2s(upper ? E.a_up : E.a_dn);
+  P2 QX = p2s(0.f), XZ = p2s(0.f);
+  if (SPHERE) {
+    QX = p2s(R.cb * E.xax + R.sb * E.xay);
+    XZ = p2s(E.xaz);
+  }
+  P2 esc = p2s(0.f);
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const P2 k1 = fma2(R.st[i], A1, R.ct[i] * NFST);
+    const P2 k2 = R.st[i] * SD;
+    const P2 k3 = fma2(R.st[i], A3, R.ct[i] * FCT);
+    P2 s2 = fma2(k1, k1, k2 * k2);
+    // An RT bin exactly along the photon direction has probability zero; the clamp only
+    // keeps the arithmetic finite there.
+    s2.v.x = fmaxf(s2.v.x, 1e-30f);
+    s2.v.y = fmaxf(s2.v.y, 1e-30f);
+    const P2 r = p2(rsqrt_approx(s2.v.x), rsqrt_approx(s2.v.y));
+    const P2 cpk = k1 * r, spk = k2 * r, stk = s2 * r;
+    const P2 c2 = (cpk + spk) * fma2(spk, M1, cpk);
+    const P2 srn = spk * cpk;  // -sr / 2
+    const P2 q = fma2(c2, PI1, srn * M2I2);
+    const P2 u = fma2(c2, PI2, srn * P2I1);
+    const P2 cpsi = fma2(spk, BQ, cpk * CD);
+    const P2 spsi = fma2(k3, fma2(spk, CD, cpk * NBQ), stk * C4);
+    const P2 c2p = (cpsi + spsi) * fma2(spsi, M1, cpsi);
+    const P2 s2p = (spsi * cpsi) * p2s(2.0f);
+    P2 p11, p12, p33, p34;
+    if (MIE) {
+      const float th0 = acos_as4446(k3.v.x), th1 = acos_as4446(k3.v.y);
+      const P2 sn = p2(th0, th1) * p2s(scale);
+      int i0 = min((int)sn.v.x, ntheta - 1), i1 = min((int)sn.v.y, ntheta - 1);
+      const P2 f = fma2(p2((float)i0, (float)i1), M1, sn);
+      const float4 a0 = F[i0], b0 = F[i0 + 1], a1 = F[i1], b1 = F[i1 + 1];
+      p11 = fma2(f, p2(b0.x - a0.x, b1.x - a1.x), p2(a0.x, a1.x));
+      p12 = fma2(f, p2(b0.y - a0.y, b1.y - a1.y), p2(a0.y, a1.y));
+      p33 = fma2(f, p2(b0.z - a0.z, b1.z - a1.z), p2(a0.z, a1.z));
+      p34 = fma2(f, p2(b0.w - a0.w, b1.w - a1.w), p2(a0.w, a1.w));
+    } else {
+      const P2 m2 = k3 * k3;
+      p11 = fma2(m2, p2s(0.75f), p2s(0.75f));
+      p12 = fma2(m2, p2s(0.75f), p2s(-0.75f));
+      p33 = k3 * p2s(1.5f);
+      p34 = p2s(0.f);
+    }
+    const P2 o0 = fma2(p11, PI0, p12 * q);
+    const P2 o1 = fma2(p12, PI0, p11 * q);
+    P2 o2, o3;
+    if (MIE) {
+      o2 = fma2(p33, u, p34 * PI3);
+      o3 = fma2(p33, PI3, (p34 * u) * M1);
+    } else {
+      o2 = p33 * u;
+      o3 = p33 * PI3;
+    }
+    const P2 r1 = fma2(c2p, o1, s2p * o2);
+    const P2 r2 = fma2(c2p, o2, (s2p * o1) * M1);
+    P2 t2;
+    if (SPHERE) {
+      const P2 kx = fma2(R.st[i], QX, R.ct[i] * XZ);
+      t2 = p2(sphere_t(kx.v.x, E.Da), sphere_t(kx.v.y, E.Da)) * p2s((float)LOG2E_D);
+    } else {
+      t2 = A * R.g[i];
+    }
+    const P2 ex = p2(t2.v.x <= tau0l ? MT<float>::exp2n(t2.v.x) : 0.f,
+                     t2.v.y <= tau0l ? MT<float>::exp2n(t2.v.y) : 0.f);
+    const P2 wgt = ex * R.w[i];
+    R.acc[i][0] = fma2(o0, wgt, R.acc[i][0]);
+    R.acc[i][1] = fma2(r1, wgt, R.acc[i][1]);
+    R.acc[i][2] = fma2(r2, wgt, R.acc[i][2]);
+    R.acc[i][3] = fma2(o3, wgt, R.acc[i][3]);
+    esc = fma2(o0, wgt, esc);
+  }
+  return esc.v.x + esc.v.y;
+}
+
+template <int NB, int BS>
+__device__ void rt_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int tile, bool upper, int pc,
+                           int q0, int q1) {
+  static_assert(NB % 2 == 0, "bins are paired");
+  constexpr int NP = NB / 2;
+  const int lane = threadIdx.x & 31;
+  const int r0 = upper ? B.up0 : B.lo0, r1 = upper ? B.up1 : B.lo1;
+  const int ngrp = (r1 - r0 + NB - 1) / NB;
+  const int item = tile * 32 + lane;
+  const bool lane_ok = item < ngrp * B.nphi;
+  const int it = lane_ok ? item : 0;
+  const int j2 = it % B.nphi, grp = it / B.nphi;
+  RTLaneF2<NP> R;
+  R.cb = B.cp[j2];
+  R.sb = B.sp[j2];
+  float st[NB], ct[NB], g[NB], w[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    int j1 = r0 + grp * NB + i;
+    bool ok = lane_ok && j1 < r1;
+    int jj = ok ? j1 : r0;
+    st[i] = B.st[jj];
+    ct[i] = B.ct[jj];
+    g[i] = B.g[jj];
+    w[i] = ok ? B.w[jj] : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    R.st[i] = p2(st[2 * i], st[2 * i + 1]);
+    R.ct[i] = p2(ct[2 * i], ct[2 * i + 1]);
+    R.g[i] = p2(g[2 * i], g[2 * i + 1]);
+    R.w[i] = p2(w[2 * i], w[2 * i + 1]);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) R.acc[i][s] = p2s(0.f);
+  }
+  const DevInstance& in = sh.inst;
+  const float tau0l = (float)(in.tau0 * LOG2E_D);
+  const int li = upper ? 0 : 1;
+  float* escarr = upper ? sh.esc_up : sh.esc_dn;
+  const bool sphere = in.geom == 1;
+  for (int q = q0; q < q1; ++q) {
+    const int e = sh.list[li][q];
+    const EventP<float>& E = sh.ev[e];
+    const DevScatterer& sc = in.scat[E.layer];
+    float esc;
+    if (sc.kind == 1) {
+      const float scale = table_scale<float>(sc);
+      esc = sphere ? rt_event_f2<NP, true, true>(R, E, sc.F, sc.ntheta, scale, tau0l, upper)
+                   : rt_event_f2<NP, true, false>(R, E, sc.F, sc.ntheta, scale, tau0l, upper);
+    } else {
+      esc = sphere ? rt_event_f2<NP, false, true>(R, E, sc.F, sc.ntheta, 0.f, tau0l, upper)
+                   : rt_event_f2<NP, false, false>(R, E, sc.F, sc.ntheta, 0.f, tau0l, upper);
+    }
+    esc = warp_sum(esc);
+    if (lane == 0) atomicAdd(&escarr[e], esc);
+  }
+  if (lane_ok) {
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      int j1 = r0 + grp * NB + i;
+      if (j1 < r1) {
+        double* dst = in.Irt + 4 * ((size_t)j2 * B.ntheta + j1);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const float2 a = R.acc[i / 2][s].v;
+          atomicAdd(dst + s, (double)((i & 1) ? a.y : a.x));
+        }
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ collect: CB tile
 template <typename T, int NB>
 struct CBLane {
@@ -953,11 +1134,17 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
         } else if (w < icb + iup) {
           w -= icb;
           const int c = w % cup;
-          rt_tile<T, NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
+          if constexpr (std::is_same<T, float>::value)
+            rt_tile_f2<NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
+          else
+            rt_tile<T, NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
         } else {
           w -= icb + iup;
           const int c = w % cdn;
-          rt_tile<T, NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
+          if constexpr (std::is_same<T, float>::value)
+            rt_tile_f2<NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
+          else
+            rt_tile<T, NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
         }
       }
     }
