@@ -53,7 +53,13 @@ def parse():
     ap.add_argument("--batch", type=int, default=1 << 22, help="photons per step per GPU")
     ap.add_argument("--fp64-sample", type=int, default=1 << 16)
     ap.add_argument("--cpu-sample", type=int, default=2000)
-    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 and CPU legs")
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64, CPU and serving legs")
+    ap.add_argument("--case", type=int, default=0,
+                    help="run one FP32 launch of the workload with this many photons and exit "
+                         "(the small case for ncu captures)")
+    ap.add_argument("--case-precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--serve-requests", type=int, default=256)
+    ap.add_argument("--serve-scale", type=float, default=1e-3, help="photon budget multiplier of the stream")
     return ap.parse_args()
 
 
@@ -108,6 +114,56 @@ class Clocks:
         loaded = [s for s in sm if s >= 0.5 * top] or sm
         return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def serve_leg(M, ctx, n_req, scale, rate_hz=200.0, seed=5):
+    """The serving stream: Poisson arrivals at rate_hz of requests drawn like the
+    4096-request mix (plane 70% / sphere 30%, optical size log-uniform in [0.1, 50],
+    albedo uniform in [0.5, 0.9999], Rayleigh or Mie with x in U[0.5, 10], n in
+    U[1.3, 1.6], k log-uniform in [1e-5, 1e-2] on 1801 angles, photon budgets
+    log-uniform in [1e4, 1e7]) with the budgets multiplied by `scale` so the stream
+    fits a short run; admission cap 20 GB."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n_req):
+        if rng.random() < 0.5:
+            sc = M.RayleighScatterer(rng.uniform(0.5, 0.9999), 1.0)
+        else:
+            x = rng.uniform(0.5, 10.0)
+            m = complex(rng.uniform(1.3, 1.6), 10 ** rng.uniform(-5, -2))
+            sc = M.MieScatterer(x / (2 * math.pi), m, 1.0, 0.1, Ntheta=1801)
+        size = 10 ** rng.uniform(-1, math.log10(50))
+        omega = rng.uniform(0.5, 0.9999)
+        if rng.random() < 0.7:
+            g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=size * sc.kl, scatterer=sc, omega=omega)])
+        else:
+            g = M.SphereGeometry(R=size * sc.kl, scatterer=sc, omega=omega)
+        n = max(1, int(round(10 ** rng.uniform(4, 7) * scale)))
+        reqs.append((M.Config(g, number_of_rays=n), g, n))
+    srv = M.Server(ctx=ctx, memory_cap_bytes=20e9, precision="fp32")
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, n_req))
+    t0 = time.perf_counter()
+    tickets = []
+    for k, (cfg, g, n) in enumerate(reqs):
+        delay = arrivals[k] - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(srv.submit(cfg, g, [1.0, 0.0, 0.0, 0.0], n, seed=seed, instance=k))
+    lat, first, last, photons = [], math.inf, 0.0, 0
+    for t, (cfg, g, n) in zip(tickets, reqs):
+        info = srv.result(t)[4]
+        lat.append(info["completed_s"] - info["submitted_s"])
+        first = min(first, info["submitted_s"])
+        last = max(last, info["completed_s"])
+        photons += n
+    st = srv.stats()
+    srv.close()
+    lat = np.array(lat)
+    return {"requests": n_req, "arrival_rate_hz": rate_hz, "budget_scale": scale,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "paths_per_s": photons / (last - first), "photons": photons, "waves": st["waves"],
+            "gpu_busy_s": st["busy_s"], "peak_resident_bytes": st["peak_resident_bytes"],
+            "memory_cap_bytes": 20e9}
 
 
 def cpu_oracle_rate(M, n_sample, threads=0):
@@ -171,8 +227,20 @@ def main():
             dist.destroy_process_group()
         return
 
-    import torch
     import mcrt_gb300 as M
+
+    if args.case > 0:
+        mie, g, cfg = workload(M, args.case)
+        out = M.simulate(cfg, g, [1.0, 0.0, 0.0, 0.0], precision=args.case_precision, seed=2,
+                         block_size=256, blocks_per_sm=2 if args.case_precision == "fp32" else 1,
+                         table_staging="shared", with_extras=True)
+        st = out[7]["stats"]
+        print(json.dumps({"case_photons": args.case, "kernel_ms": st["kernel_ms"],
+                          "paths_per_s": args.case / st["kernel_ms"] * 1e3, "events": st["events"],
+                          "rt_evals": st["rt_evals"], "cbn_evals": st["cbn_evals"], "cb1_evals": st["cb1_evals"]}))
+        return
+
+    import torch
 
     ctx = M.Context(local)
     mie, g, cfg = workload(M, args.batch)
@@ -276,7 +344,9 @@ def main():
         v64 = np64 / (r64["stats"]["kernel_ms"] / 1e3)
         vplain = n64 / (rp["stats"]["kernel_ms"] / 1e3)
         cpu_v, cores, cpu_dt = cpu_oracle_rate(M, args.cpu_sample)
+        serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
         extras = {
+            "serve": serve,
             "fp64_persistent": {"value": v64, "unit": "paths/s", "sample_photons": np64},
             "fp64_plain": {"value": vplain, "unit": "paths/s", "sample_photons": n64,
                            "threads": plain_threads},

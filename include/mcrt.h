@@ -125,9 +125,10 @@ typedef struct {
   uint32_t instance;    /* Philox key word (one per simulate call of a run_rt) */
   int rng_mode;         /* mcrt_rng_mode */
   int64_t photon_begin; /* first photon index (sub-runs continue a stream) */
-  int block_size;       /* persistent: 0 = autotuned; 128, 256 or 512 */
-  int blocks_per_sm;    /* persistent: 0 = autotuned */
+  int block_size;       /* persistent: 0 = autotuned; FP32 256, 512, 768 (or 128); FP64 128, 256 */
+  int blocks_per_sm;    /* persistent: 0 = autotuned (or the most that fit) */
   int plain_threads;    /* plain: 0 = min(maximum_threads, number_of_rays) */
+  int table_staging;    /* persistent: 0 = autotuned, 1 = shared memory, 2 = global memory (L1) */
 } mcrt_run_opts;
 
 /* Diagnostics returned beside the tallies (all raw sums over the photons run). */
@@ -213,6 +214,57 @@ int mcrt_batch_read(mcrt_batch* b, int i, double A_out[5], double* Irt, double* 
 /* Device time of the last launch and the total photons it ran. */
 int mcrt_batch_timing(mcrt_batch* b, double* kernel_ms, double* photons);
 int mcrt_batch_destroy(mcrt_batch* b);
+
+/* ------------------------------------------------------------------ serving loop */
+/* A continuous-batching request loop in front of the persistent kernel. Requests (each
+ * a simulate() instance with its own config, geometry, scatterers, I0, seed and photon
+ * budget) are admitted while the resident device footprint (the request's Mie tables,
+ * bin tables and tallies) stays under memory_cap_bytes and fewer than max_active are
+ * resident; their state stays on the device until they finish. A worker thread runs
+ * waves: each wave is one persistent launch in which every active request processes up
+ * to its share of wave_photons photons, replayed from a captured CUDA graph; requests
+ * that arrive while a wave runs join a following wave, so their work overlaps others'
+ * on the device. Each request's photons are fixed by its (seed, instance) streams and
+ * photon indices, so its result does not depend on what it ran beside. */
+typedef struct {
+  double memory_cap_bytes; /* admission cap on the resident footprint (0 = 20e9) */
+  int max_active;          /* most requests resident at once (0 = 256) */
+  int64_t wave_photons;    /* photons per wave, shared by the active requests (0 = 1<<20) */
+  int64_t min_quantum;     /* at least this many photons per request per wave (0 = 4096) */
+  int precision;           /* mcrt_precision */
+  int use_graphs;          /* 0 = direct launches, 1 = replay captured CUDA graphs */
+} mcrt_server_opts;
+
+typedef struct {
+  const mcrt_config* config;
+  const mcrt_geometry* geometry;
+  double I0[4];
+  uint64_t seed;
+  uint32_t instance;
+  int64_t n_photons;
+} mcrt_request;
+
+typedef struct {
+  double submitted_s, admitted_s, completed_s; /* on the server's monotonic clock */
+  double footprint_bytes;
+  int64_t photons;
+  int waves;      /* waves the request took part in */
+  int status_flags;
+} mcrt_ticket_info;
+
+int mcrt_server_create(mcrt_ctx* ctx, const mcrt_server_opts* opts, mcrt_server** out);
+/* Copies the request (the scatterers must outlive it) and queues it; returns a ticket. */
+int mcrt_server_submit(mcrt_server* s, const mcrt_request* r, uint64_t* ticket);
+/* MCRT_OK once the ticket's result is ready, MCRT_ETIMEDOUT if not within timeout_ms. */
+int mcrt_server_wait(mcrt_server* s, uint64_t ticket, double timeout_ms);
+/* The result divided by the request's photon count (as mcrt_simulate returns it), then
+ * releases the ticket; any output pointer may be NULL. */
+int mcrt_server_result(mcrt_server* s, uint64_t ticket, double A_out[5], double* Irt, double* Icb,
+                       double* Icb_ladder, mcrt_ticket_info* info);
+/* out[0..7] = completed, photons completed, waves, busy seconds, peak resident bytes,
+ * resident bytes, pending, active. */
+int mcrt_server_stats(mcrt_server* s, double out[8]);
+int mcrt_server_destroy(mcrt_server* s);
 
 /* ------------------------------------------------------------------ no device allocation */
 /* Size of the device array that mcrt_simulate_noalloc works in (24 MiB). */

@@ -3,13 +3,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "mcrt.h"
@@ -72,7 +76,11 @@ struct mcrt_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::mutex mu;
-  std::map<std::string, std::pair<int, int>> tuned;  // signature -> (block size, blocks/SM)
+  struct Tuned {
+    int bs, bpsm, staging;
+    double paths_per_ms;
+  };
+  std::map<std::string, Tuned> tuned;  // workload signature -> fastest launch shape
 };
 
 struct mcrt_scatterer {
@@ -506,6 +514,8 @@ int table_f4_of(const DevInstance& D) {
 }  // namespace
 
 // ================================================================== launches
+using ctx_t = mcrt_ctx;
+
 struct Launch {
   int precision = MCRT_FP32, kernel = MCRT_KERNEL_PERSISTENT;
   int bs = 256, bpsm = 0, blocks = 0;
@@ -543,12 +553,17 @@ int size_launch(mcrt_ctx* ctx, Group& G, const mcrt_run_opts* o, const std::stri
   if (L.kernel == MCRT_KERNEL_PLAIN) return MCRT_OK;
   int bs = o && o->block_size ? o->block_size : 0;
   int bpsm = o && o->blocks_per_sm ? o->blocks_per_sm : 0;
-  if (!bs) {
+  int staging = o ? o->table_staging : 0;
+  if (staging < 0 || staging > 2) return set_err(MCRT_EINVAL, "table_staging must be 0, 1 or 2");
+  {
     std::lock_guard<std::mutex> lk(ctx->mu);
     auto it = ctx->tuned.find(sig);
     if (it != ctx->tuned.end()) {
-      bs = it->second.first;
-      if (!bpsm) bpsm = it->second.second;
+      if (!bs) {
+        bs = it->second.bs;
+        if (!bpsm) bpsm = it->second.bpsm;
+      }
+      if (!staging) staging = it->second.staging;
     }
   }
   if (!bs) bs = L.precision == MCRT_FP32 ? 256 : 128;
@@ -556,7 +571,8 @@ int size_launch(mcrt_ctx* ctx, Group& G, const mcrt_run_opts* o, const std::stri
   if (!kernel_info(L.precision, bs, ki))
     return set_err(MCRT_EINVAL, "unsupported block size for this precision (FP32: 128/256/512/768, FP64: 128/256)");
   int tf4 = 0;
-  for (auto& D : G.hinst) tf4 = std::max(tf4, table_f4_of(D));
+  if (staging != 2)  // 2: Mie tables stay in global memory and are read through L1
+    for (auto& D : G.hinst) tf4 = std::max(tf4, table_f4_of(D));
   size_t smem = ki.shared_static + (size_t)tf4 * 16;
   if (smem > (size_t)ctx->smem_optin) {
     // the tables that do not fit are read from global memory through L1
@@ -577,6 +593,10 @@ int size_launch(mcrt_ctx* ctx, Group& G, const mcrt_run_opts* o, const std::stri
   return MCRT_OK;
 }
 
+int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const double* I0, uint64_t seed,
+             uint32_t inst, long long nph, long long photon_begin, int rng_mode, const mcrt_run_opts* o,
+             const std::string& sig);
+
 // Allocates tallies, counters, bins and state for the group's instances.
 int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const* geoms,
                 const double (*I0)[4], const uint64_t* seeds, const uint32_t* insts,
@@ -596,10 +616,25 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
   for (int i = 0; i < n; ++i) G.order[i] = i;
   std::stable_sort(G.order.begin(), G.order.end(),
                    [&](int a, int b) { return G.hinst[a].n_photons > G.hinst[b].n_photons; });
-  std::string sig = std::to_string(geoms[0]->kind) + "/" + std::to_string(c->n_theta) + "x" +
+  const DevInstance& D0 = G.hinst[G.order[0]];
+  std::string sig = std::to_string(D0.geom) + "/" + std::to_string(c->n_theta) + "x" +
                     std::to_string(c->n_phi) + "/" + std::to_string(c->n_theta_b) + "x" +
-                    std::to_string(c->n_phi_b) + "/" + std::to_string(G.hinst[0].scat[0].kind) +
-                    "/" + std::to_string(o ? o->precision : 0);
+                    std::to_string(c->n_phi_b) + "/" + std::to_string(D0.scat[0].kind) + ":" +
+                    std::to_string(D0.scat[0].ntheta) + "/" + std::to_string(o ? o->precision : 0);
+  const bool persistent = !o || o->kernel == MCRT_KERNEL_PERSISTENT;
+  if (persistent && (!o || !o->block_size || !o->table_staging)) {
+    bool have;
+    {
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      have = ctx->tuned.count(sig) > 0;
+    }
+    if (!have) {
+      const int big = G.order[0];
+      int rc = autotune(ctx, c, geoms[big], I0[big], seeds[big], insts[big], nph[big], photon_begin,
+                        rng_mode, o, sig);
+      if (rc) return rc;
+    }
+  }
   int rc = size_launch(ctx, G, o, sig);
   if (rc) return rc;
   // bin tables, one per distinct (geometry kind, incidence)
@@ -732,6 +767,62 @@ int read_instance(Group& G, int user_index, double A_out[5], double* Irt, double
     stats->block_size = G.L.kernel == MCRT_KERNEL_PERSISTENT ? G.L.bs : 256;
     stats->blocks = G.L.kernel == MCRT_KERNEL_PERSISTENT ? G.L.blocks : (int)((G.plain_threads + 255) / 256);
   }
+  return MCRT_OK;
+}
+
+// The autotuner: times the candidate launch shapes (threads per block, blocks per SM)
+// and, for Mie scatterers, the table staging (shared memory or global memory through
+// L1) on a sample of the workload's own photons, two per thread, and keeps the fastest
+// for this workload signature in the context. User-given fields are kept fixed.
+int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const double* I0, uint64_t seed,
+             uint32_t inst, long long nph, long long photon_begin, int rng_mode, const mcrt_run_opts* o,
+             const std::string& sig) {
+  const int prec = o ? o->precision : MCRT_FP32;
+  std::vector<std::pair<int, int>> shapes;
+  if (prec == MCRT_FP32)
+    shapes = {{256, 2}, {256, 1}, {512, 1}, {768, 1}};
+  else
+    shapes = {{128, 2}, {128, 1}, {256, 1}};
+  if (o && o->block_size) {
+    shapes.clear();
+    shapes.push_back({o->block_size, o->blocks_per_sm});
+  }
+  bool mie = false;
+  for (int l = 0; l < g->n_layers; ++l) mie = mie || g->layers[l].scatterer->kind == MCRT_MIE;
+  std::vector<int> stagings = mie ? std::vector<int>{1, 2} : std::vector<int>{1};
+  if (o && o->table_staging) stagings = {o->table_staging};
+  const double I[1][4] = {{I0[0], I0[1], I0[2], I0[3]}};
+  ctx_t::Tuned best{0, 0, 0, -1.0};
+  std::vector<std::string> seen;
+  bool warmed = false;
+  for (auto sh : shapes) {
+    for (int st : stagings) {
+      mcrt_run_opts oo{};
+      if (o) oo = *o;
+      oo.kernel = MCRT_KERNEL_PERSISTENT;
+      oo.block_size = sh.first;
+      oo.blocks_per_sm = sh.second;
+      oo.table_staging = st;
+      const long long ns = std::max<long long>(1, std::min<long long>(nph, 2LL * ctx->sms * sh.first *
+                                                                          std::max(sh.second, 1)));
+      Group T;
+      const mcrt_geometry* gs[1] = {g};
+      long long n1 = ns;
+      if (build_group(ctx, c, gs, I, &seed, &inst, &n1, photon_begin, rng_mode, 1, &oo, T)) continue;
+      std::string key = std::to_string(T.L.bs) + "x" + std::to_string(T.L.bpsm) + "/" + std::to_string(T.L.table_f4);
+      if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;  // occupancy folded it
+      seen.push_back(key);
+      for (int rep = warmed ? 1 : 0; rep < 2; ++rep) {  // the first launch also warms up the device
+        if (launch_group(T) || finish_group(T)) return MCRT_ECUDA;
+      }
+      warmed = true;
+      const double rate = ns / std::max(T.last_ms, 1e-3f);
+      if (rate > best.paths_per_ms) best = ctx_t::Tuned{T.L.bs, T.L.bpsm, st, rate};
+    }
+  }
+  if (best.bs == 0) return set_err(MCRT_EINVAL, "autotune: no launch shape fits this workload");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->tuned[sig] = best;
   return MCRT_OK;
 }
 
@@ -929,6 +1020,480 @@ extern "C" int mcrt_measure_fp32_peak(mcrt_ctx* ctx, double* tflops) {
   }
   const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
   *tflops = flops / (best * 1e-3) / 1e12;
+  return MCRT_OK;
+}
+
+// ================================================================== serving loop
+// Continuous batching in front of the persistent kernel (declared in include/mcrt.h).
+namespace {
+
+// Bin tables laid out for a given device address (defined with the no-allocation path).
+template <typename T>
+std::vector<unsigned char> pack_bins_at(const HostBins& H, const unsigned char* dev);
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Device memory owned by one resident request, released stream-ordered so that freeing
+// never waits for the wave still running on the device.
+struct AsyncBuf {
+  void* p = nullptr;
+  cudaStream_t st = nullptr;
+  ~AsyncBuf() {
+    if (p) cudaFreeAsync(p, st);
+  }
+};
+
+struct SrvReq {
+  uint64_t id = 0;
+  mcrt_config cfg{};
+  std::vector<double> arrays[9];
+  mcrt_geometry geom{};
+  std::vector<mcrt_layer> layers;
+  double I0[4] = {0, 0, 0, 0};
+  uint64_t seed = 0;
+  uint32_t inst = 0;
+  long long nph = 0;
+  DevInstance D{};
+  std::vector<unsigned char> binbytes;
+  AsyncBuf tally, bins;
+  size_t nrt = 0, ncb = 0, per_inst = 0;
+  double footprint = 0;
+  long long next = 0;       // next photon index to hand to a wave
+  long long last_wave = -1; // last wave that carried photons of this request
+  int waves = 0;
+  int state = 0;            // 0 pending, 1 resident, 2 done, 3 failed
+  unsigned status = 0;
+  double t_sub = 0, t_adm = 0, t_done = 0;
+  std::vector<double> result;  // raw sums once done
+};
+
+}  // namespace
+
+struct mcrt_server {
+  mcrt_ctx* ctx = nullptr;
+  mcrt_server_opts o{};
+  KInfo ki{};
+  int bs = 256, blocks = 0, tf4 = 0;
+  size_t smem = 0;
+  cudaStream_t stream = nullptr;
+  struct Slot {
+    DevBuf d_wave, d_claim, d_status, d_state, d_tacc;
+    DevInstance* h_wave = nullptr;  // pinned; read by the wave's copy when it runs
+    cudaGraphExec_t gexec = nullptr;
+    cudaEvent_t start = nullptr, done = nullptr;
+    long long wave_id = -1;
+    std::vector<SrvReq*> members;
+    bool in_flight = false;
+  } slot[2];
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv;
+  bool stop = false;
+  int fatal = 0;
+  std::string fatal_msg;
+  uint64_t next_id = 1;
+  long long next_wave = 0;
+  std::deque<SrvReq*> pending;
+  std::vector<SrvReq*> active;
+  std::map<uint64_t, std::unique_ptr<SrvReq>> reqs;
+  double resident = 0, peak_resident = 0, busy_s = 0, completed = 0, photons_done = 0;
+};
+
+namespace {
+
+// Footprint of a request: its tallies, bin tables and Mie tables.
+double request_footprint(const SrvReq& r) {
+  double b = (double)r.per_inst * sizeof(double) + (double)r.binbytes.size() + 4096.0;
+  for (int s = 0; s < r.D.n_scat; ++s)
+    if (r.D.scat[s].kind == 1) b += 32.0 * (r.D.scat[s].ntheta + 1) + 4.0 * (r.D.scat[s].rp + 4);
+  return b;
+}
+
+// Admits pending requests while the cap and slot count allow (under the lock).
+int srv_admit(mcrt_server* S) {
+  while (!S->pending.empty() && (int)S->active.size() < S->o.max_active) {
+    SrvReq* r = S->pending.front();
+    if (S->resident + r->footprint > S->o.memory_cap_bytes && !S->active.empty()) break;
+    S->pending.pop_front();
+    r->tally.st = r->bins.st = S->stream;
+    if (cudaMallocAsync(&r->tally.p, r->per_inst * sizeof(double), S->stream) != cudaSuccess ||
+        cudaMallocAsync(&r->bins.p, r->binbytes.size(), S->stream) != cudaSuccess)
+      return set_err(MCRT_ENOMEM, "server: device allocation for a request failed");
+    // bin tables carry absolute pointers: rebuild them for the final address
+    HostBins H = make_bins(&r->cfg, r->geom.kind,
+                           host::Sph{r->D.kfs[0], r->D.kfs[1], r->D.kfs[2], r->D.kfs[3]});
+    r->binbytes = S->o.precision == MCRT_FP32 ? pack_bins_at<float>(H, (unsigned char*)r->bins.p)
+                                              : pack_bins_at<double>(H, (unsigned char*)r->bins.p);
+    CK(cudaMemcpyAsync(r->bins.p, r->binbytes.data(), r->binbytes.size(), cudaMemcpyHostToDevice, S->stream));
+    CK(cudaMemsetAsync(r->tally.p, 0, r->per_inst * sizeof(double), S->stream));
+    double* t = (double*)r->tally.p;
+    r->D.bins = r->bins.p;
+    r->D.Irt = t;
+    r->D.Icb = t + r->nrt;
+    r->D.ladder = t + r->nrt + r->ncb;
+    r->D.acc = t + r->nrt + r->ncb + r->ncb / 4;
+    r->state = 1;
+    r->t_adm = now_s();
+    S->active.push_back(r);
+    S->resident += r->footprint;
+    S->peak_resident = std::max(S->peak_resident, S->resident);
+  }
+  return MCRT_OK;
+}
+
+// Waits for the wave in slot b and retires the requests whose last photons it carried.
+int srv_retire(mcrt_server* S, int b) {
+  auto& sl = S->slot[b];
+  if (!sl.in_flight) return MCRT_OK;
+  CK(cudaEventSynchronize(sl.done));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, sl.start, sl.done);
+  unsigned status = 0;
+  CK(cudaMemcpy(&status, sl.d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  std::vector<SrvReq*> finished;
+  for (SrvReq* r : sl.members) {
+    r->status |= status;
+    if (r->last_wave == sl.wave_id && r->next >= r->nph) finished.push_back(r);
+  }
+  for (SrvReq* r : finished) {
+    r->result.resize(r->per_inst);
+    CK(cudaMemcpyAsync(r->result.data(), r->tally.p, r->per_inst * sizeof(double), cudaMemcpyDeviceToHost,
+                       S->stream));
+  }
+  CK(cudaStreamSynchronize(S->stream));
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->busy_s += ms * 1e-3;
+  for (SrvReq* r : finished) {
+    r->tally.~AsyncBuf();
+    new (&r->tally) AsyncBuf();
+    r->bins.~AsyncBuf();
+    new (&r->bins) AsyncBuf();
+    r->state = 2;
+    r->t_done = now_s();
+    S->resident -= r->footprint;
+    S->completed += 1;
+    S->photons_done += (double)r->nph;
+    S->active.erase(std::find(S->active.begin(), S->active.end(), r));
+  }
+  sl.in_flight = false;
+  sl.members.clear();
+  S->cv.notify_all();
+  return MCRT_OK;
+}
+
+int srv_launch(mcrt_server* S, int b) {
+  auto& sl = S->slot[b];
+  if (S->o.use_graphs) {
+    CK(cudaEventRecord(sl.start, S->stream));
+    CK(cudaGraphLaunch(sl.gexec, S->stream));
+    CK(cudaEventRecord(sl.done, S->stream));
+  } else {
+    CK(cudaEventRecord(sl.start, S->stream));
+    CK(cudaMemcpyAsync(sl.d_wave.p, sl.h_wave, S->o.max_active * sizeof(DevInstance), cudaMemcpyHostToDevice,
+                       S->stream));
+    CK(cudaMemsetAsync(sl.d_claim.p, 0, sl.d_claim.n, S->stream));
+    CK(cudaMemsetAsync(sl.d_status.p, 0, sl.d_status.n, S->stream));
+    KParams p{sl.d_wave.as<const DevInstance>(), S->o.max_active, sl.d_state.as<uint4>(),
+              sl.d_tacc.as<double>(), sl.d_status.as<unsigned>(), S->tf4};
+    CK(launch_transport(S->ki, S->blocks, S->bs, S->smem, S->stream, p));
+    CK(cudaEventRecord(sl.done, S->stream));
+  }
+  sl.in_flight = true;
+  return MCRT_OK;
+}
+
+// Builds the next wave in slot b from the resident requests with photons left.
+int srv_build_wave(mcrt_server* S, int b, bool& launched) {
+  launched = false;
+  auto& sl = S->slot[b];
+  std::vector<SrvReq*> members;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (SrvReq* r : S->active)
+      if (r->next < r->nph) members.push_back(r);
+  }
+  if (members.empty()) return MCRT_OK;
+  std::stable_sort(members.begin(), members.end(),
+                   [](SrvReq* a, SrvReq* c) { return a->nph - a->next > c->nph - c->next; });
+  const long long q = std::max<long long>(S->o.min_quantum, S->o.wave_photons / (long long)members.size());
+  const long long wid = S->next_wave++;
+  for (int i = 0; i < S->o.max_active; ++i) {
+    DevInstance& W = sl.h_wave[i];
+    if (i < (int)members.size()) {
+      SrvReq* r = members[i];
+      W = r->D;
+      W.photon_begin = r->next;
+      W.n_photons = std::min<long long>(q, r->nph - r->next);
+      r->next += W.n_photons;
+      r->last_wave = wid;
+      r->waves += 1;
+    } else {
+      W.n_photons = 0;  // padding: skipped by the kernel
+    }
+    W.claim = sl.d_claim.as<unsigned long long>() + i;
+  }
+  sl.members = members;
+  sl.wave_id = wid;
+  int rc = srv_launch(S, b);
+  if (rc) return rc;
+  launched = true;
+  return MCRT_OK;
+}
+
+void srv_fail(mcrt_server* S, int rc) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->fatal = rc;
+  S->fatal_msg = g_err;
+  for (auto& kv : S->reqs)
+    if (kv.second->state < 2) kv.second->state = 3;
+  S->cv.notify_all();
+}
+
+void srv_loop(mcrt_server* S) {
+  cudaSetDevice(S->ctx->device);
+  int cur = 0;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      if (S->stop) break;
+      int rc = srv_admit(S);
+      if (rc) {
+        lk.unlock();
+        srv_fail(S, rc);
+        return;
+      }
+      if (S->active.empty() && !S->slot[0].in_flight && !S->slot[1].in_flight) {
+        S->cv.wait_for(lk, std::chrono::milliseconds(5));
+        continue;
+      }
+    }
+    // Slot cur held the wave before last; retire it, then refill it, so one wave always
+    // waits queued behind the running one.
+    int rc = srv_retire(S, cur);
+    if (rc) return srv_fail(S, rc);
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      rc = srv_admit(S);
+    }
+    if (rc) return srv_fail(S, rc);
+    bool launched = false;
+    rc = srv_build_wave(S, cur, launched);
+    if (rc) return srv_fail(S, rc);
+    if (!launched) {
+      rc = srv_retire(S, cur ^ 1);
+      if (rc) return srv_fail(S, rc);
+    }
+    cur ^= 1;
+  }
+  srv_retire(S, 0);
+  srv_retire(S, 1);
+}
+
+}  // namespace
+
+extern "C" int mcrt_server_create(mcrt_ctx* ctx, const mcrt_server_opts* opts, mcrt_server** out) {
+  if (!ctx || !out) return set_err(MCRT_EINVAL, "mcrt_server_create: NULL argument");
+  *out = nullptr;
+  std::unique_ptr<mcrt_server> S(new mcrt_server());
+  S->ctx = ctx;
+  if (opts) S->o = *opts;
+  if (S->o.memory_cap_bytes <= 0) S->o.memory_cap_bytes = 20e9;
+  if (S->o.max_active <= 0) S->o.max_active = 256;
+  if (S->o.wave_photons <= 0) S->o.wave_photons = 1 << 20;
+  if (S->o.min_quantum <= 0) S->o.min_quantum = 4096;
+  if (S->o.precision != MCRT_FP32 && S->o.precision != MCRT_FP64)
+    return set_err(MCRT_EINVAL, "precision must be MCRT_FP32 or MCRT_FP64");
+  CK(cudaSetDevice(ctx->device));
+  S->bs = S->o.precision == MCRT_FP32 ? 256 : 128;
+  kernel_info(S->o.precision, S->bs, S->ki);
+  // room for one 1801-angle Mie table set in shared memory; larger sets read through L1
+  S->tf4 = 2 * 1802 + (1002 + 3) / 4;
+  S->smem = S->ki.shared_static + (size_t)S->tf4 * 16;
+  CK(cudaFuncSetAttribute(S->ki.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->smem));
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, S->ki.fn, S->bs, S->smem));
+  if (occ < 1) return set_err(MCRT_EINVAL, "server: kernel does not fit");
+  S->blocks = ctx->sms * occ;
+  CK(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  const size_t slots = (size_t)S->blocks * S->bs;
+  for (auto& sl : S->slot) {
+    CK(sl.d_wave.alloc(S->o.max_active * sizeof(DevInstance)));
+    CK(sl.d_claim.alloc(S->o.max_active * sizeof(unsigned long long)));
+    CK(sl.d_status.alloc(sizeof(unsigned)));
+    CK(sl.d_state.alloc(slots * S->ki.state_bytes));
+    CK(sl.d_tacc.alloc(slots * NACC * sizeof(double)));
+    CK(cudaMallocHost(&sl.h_wave, S->o.max_active * sizeof(DevInstance)));
+    std::memset(sl.h_wave, 0, S->o.max_active * sizeof(DevInstance));
+    for (int i = 0; i < S->o.max_active; ++i) sl.h_wave[i].claim = sl.d_claim.as<unsigned long long>() + i;
+    CK(cudaEventCreate(&sl.start));
+    CK(cudaEventCreate(&sl.done));
+    if (S->o.use_graphs) {
+      // One graph per slot: copy the wave table, clear the counters, run the wave.
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+      cudaMemcpyAsync(sl.d_wave.p, sl.h_wave, S->o.max_active * sizeof(DevInstance), cudaMemcpyHostToDevice,
+                      S->stream);
+      cudaMemsetAsync(sl.d_claim.p, 0, sl.d_claim.n, S->stream);
+      cudaMemsetAsync(sl.d_status.p, 0, sl.d_status.n, S->stream);
+      KParams p{sl.d_wave.as<const DevInstance>(), S->o.max_active, sl.d_state.as<uint4>(), sl.d_tacc.as<double>(),
+                sl.d_status.as<unsigned>(), S->tf4};
+      launch_transport(S->ki, S->blocks, S->bs, S->smem, S->stream, p);
+      CK(cudaStreamEndCapture(S->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&sl.gexec, g, 0);
+      cudaGraphDestroy(g);
+      CK(e);
+    }
+  }
+  mcrt_server* raw = S.release();
+  raw->worker = std::thread(srv_loop, raw);
+  *out = raw;
+  return MCRT_OK;
+}
+
+extern "C" int mcrt_server_submit(mcrt_server* S, const mcrt_request* q, uint64_t* ticket) {
+  if (!S || !q || !ticket || !q->config || !q->geometry)
+    return set_err(MCRT_EINVAL, "mcrt_server_submit: NULL argument");
+  int rc = validate_geometry(q->geometry);
+  if (rc) return rc;
+  rc = validate_config(q->config, q->geometry->kind);
+  if (rc) return rc;
+  if (q->n_photons < 0) return set_err(MCRT_EINVAL, "n_photons must be >= 0");
+  std::unique_ptr<SrvReq> r(new SrvReq());
+  const mcrt_config* c = q->config;
+  r->cfg = *c;
+  const double* src[9] = {c->cos_phi, c->sin_phi, c->cos_theta, c->sin_theta, c->inorm,
+                          c->cos_theta_b, c->sin_theta_b, c->cos_phi_b, c->sin_phi_b};
+  const int len[9] = {c->n_phi, c->n_phi, c->n_theta, c->n_theta, c->n_theta,
+                      c->n_theta_b, c->n_theta_b, c->n_phi_b, c->n_phi_b};
+  for (int i = 0; i < 9; ++i) r->arrays[i].assign(src[i], src[i] + len[i]);
+  r->cfg.cos_phi = r->arrays[0].data();
+  r->cfg.sin_phi = r->arrays[1].data();
+  r->cfg.cos_theta = r->arrays[2].data();
+  r->cfg.sin_theta = r->arrays[3].data();
+  r->cfg.inorm = r->arrays[4].data();
+  r->cfg.cos_theta_b = r->arrays[5].data();
+  r->cfg.sin_theta_b = r->arrays[6].data();
+  r->cfg.cos_phi_b = r->arrays[7].data();
+  r->cfg.sin_phi_b = r->arrays[8].data();
+  r->cfg.number_of_rays = q->n_photons;
+  r->layers.assign(q->geometry->layers, q->geometry->layers + q->geometry->n_layers);
+  r->geom = *q->geometry;
+  r->geom.layers = r->layers.data();
+  for (int s = 0; s < 4; ++s) r->I0[s] = q->I0[s];
+  r->seed = q->seed;
+  r->inst = q->instance;
+  r->nph = q->n_photons;
+  host::Sph kfs;
+  rc = make_instance(&r->cfg, &r->geom, r->I0, r->seed, r->inst, 0, r->nph, 0, r->D, kfs);
+  if (rc) return rc;
+  HostBins H = make_bins(&r->cfg, r->geom.kind, kfs);
+  r->binbytes = S->o.precision == MCRT_FP32 ? pack_bins_at<float>(H, nullptr) : pack_bins_at<double>(H, nullptr);
+  r->nrt = 4 * (size_t)c->n_theta * c->n_phi;
+  r->ncb = 4 * (size_t)c->n_theta_b * c->n_phi_b;
+  r->per_inst = r->nrt + r->ncb + r->ncb / 4 + NACC;
+  r->footprint = request_footprint(*r);
+  if (r->footprint > S->o.memory_cap_bytes)
+    return set_err(MCRT_EBUSY, "request footprint exceeds the server's memory cap");
+  r->t_sub = now_s();
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (S->fatal) return set_err(S->fatal, "server stopped: " + S->fatal_msg);
+  r->id = S->next_id++;
+  *ticket = r->id;
+  if (r->nph == 0) {  // nothing to run
+    r->state = 2;
+    r->result.assign(r->per_inst, 0.0);
+    r->t_adm = r->t_done = r->t_sub;
+  } else {
+    S->pending.push_back(r.get());
+  }
+  S->reqs[r->id] = std::move(r);
+  S->cv.notify_all();
+  return MCRT_OK;
+}
+
+extern "C" int mcrt_server_wait(mcrt_server* S, uint64_t ticket, double timeout_ms) {
+  if (!S) return set_err(MCRT_EINVAL, "mcrt_server_wait: NULL server");
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return set_err(MCRT_ENOTFOUND, "unknown ticket");
+  SrvReq* r = it->second.get();
+  const auto until = std::chrono::steady_clock::now() + std::chrono::duration<double, std::milli>(timeout_ms);
+  while (r->state < 2) {
+    if (S->cv.wait_until(lk, until) == std::cv_status::timeout && r->state < 2)
+      return set_err(MCRT_ETIMEDOUT, "mcrt_server_wait: timed out");
+  }
+  if (r->state == 3) return set_err(S->fatal ? S->fatal : MCRT_ECUDA, "server failed: " + S->fatal_msg);
+  return MCRT_OK;
+}
+
+extern "C" int mcrt_server_result(mcrt_server* S, uint64_t ticket, double A_out[5], double* Irt, double* Icb,
+                                  double* lad, mcrt_ticket_info* info) {
+  if (!S) return set_err(MCRT_EINVAL, "mcrt_server_result: NULL server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return set_err(MCRT_ENOTFOUND, "unknown ticket");
+  SrvReq* r = it->second.get();
+  if (r->state != 2) return set_err(MCRT_EBUSY, "result not ready");
+  const double inv = r->nph > 0 ? 1.0 / (double)r->nph : 0.0;
+  const double* h = r->result.data();
+  const double* acc = h + r->nrt + r->ncb + r->ncb / 4;
+  if (A_out)
+    for (int s = 0; s < 5; ++s) A_out[s] = acc[s] * inv;
+  if (Irt)
+    for (size_t i = 0; i < r->nrt; ++i) Irt[i] = h[i] * inv;
+  if (Icb)
+    for (size_t i = 0; i < r->ncb; ++i) Icb[i] = h[r->nrt + i] * inv;
+  if (lad)
+    for (size_t i = 0; i < r->ncb / 4; ++i) lad[i] = h[r->nrt + r->ncb + i] * inv;
+  if (info) {
+    info->submitted_s = r->t_sub;
+    info->admitted_s = r->t_adm;
+    info->completed_s = r->t_done;
+    info->footprint_bytes = r->footprint;
+    info->photons = r->nph;
+    info->waves = r->waves;
+    info->status_flags = (int)r->status;
+  }
+  S->reqs.erase(it);
+  return MCRT_OK;
+}
+
+extern "C" int mcrt_server_stats(mcrt_server* S, double out[8]) {
+  if (!S || !out) return set_err(MCRT_EINVAL, "mcrt_server_stats: NULL argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  out[0] = S->completed;
+  out[1] = S->photons_done;
+  out[2] = (double)S->next_wave;
+  out[3] = S->busy_s;
+  out[4] = S->peak_resident;
+  out[5] = S->resident;
+  out[6] = (double)S->pending.size();
+  out[7] = (double)S->active.size();
+  return MCRT_OK;
+}
+
+extern "C" int mcrt_server_destroy(mcrt_server* S) {
+  if (!S) return MCRT_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    S->cv.notify_all();
+  }
+  if (S->worker.joinable()) S->worker.join();
+  cudaSetDevice(S->ctx->device);
+  cudaStreamSynchronize(S->stream);
+  S->reqs.clear();
+  cudaStreamSynchronize(S->stream);
+  for (auto& sl : S->slot) {
+    if (sl.gexec) cudaGraphExecDestroy(sl.gexec);
+    if (sl.h_wave) cudaFreeHost(sl.h_wave);
+    if (sl.start) cudaEventDestroy(sl.start);
+    if (sl.done) cudaEventDestroy(sl.done);
+  }
+  cudaStreamDestroy(S->stream);
+  delete S;
   return MCRT_OK;
 }
 

@@ -672,6 +672,25 @@ __device__ __forceinline__ P2 operator*(P2 a, P2 b) { return P2{__fmul2_rn(a.v, 
 __device__ __forceinline__ P2 operator+(P2 a, P2 b) { return P2{__fadd2_rn(a.v, b.v)}; }
 __device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) { return P2{__ffma2_rn(a.v, b.v, c.v)}; }
 
+// acos_as4446 (Abramowitz & Stegun 4.4.46) on two values at once.
+__device__ __forceinline__ P2 acos2(P2 x) {
+  const P2 ax = p2(fabsf(x.v.x), fabsf(x.v.y));
+  P2 p = fma2(p2s(-0.0012624911f), ax, p2s(0.0066700901f));
+  p = fma2(p, ax, p2s(-0.0170881256f));
+  p = fma2(p, ax, p2s(0.0308918810f));
+  p = fma2(p, ax, p2s(-0.0501743046f));
+  p = fma2(p, ax, p2s(0.0889789874f));
+  p = fma2(p, ax, p2s(-0.2145988016f));
+  p = fma2(p, ax, p2s(1.5707963050f));
+  P2 y = fma2(ax, p2s(-1.0f), p2s(1.0f));
+  y.v.x = fmaxf(y.v.x, 1e-30f);  // |x| = 1 gives acos = 0 or pi
+  y.v.y = fmaxf(y.v.y, 1e-30f);
+  const P2 r = (y * p2(rsqrt_approx(y.v.x), rsqrt_approx(y.v.y))) * p;
+  const P2 sg = p2(x.v.x < 0.f ? -1.f : 1.f, x.v.y < 0.f ? -1.f : 1.f);
+  const P2 off = p2(x.v.x < 0.f ? 3.14159265358979f : 0.f, x.v.y < 0.f ? 3.14159265358979f : 0.f);
+  return fma2(sg, r, off);
+}
+
 template <int NP>
 struct RTLaneF2 {
   P2 st[NP], ct[NP], g[NP], w[NP];
@@ -718,8 +737,7 @@ __device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float
     const P2 s2p = (spsi * cpsi) * p2s(2.0f);
     P2 p11, p12, p33, p34;
     if (MIE) {
-      const float th0 = acos_as4446(k3.v.x), th1 = acos_as4446(k3.v.y);
-      const P2 sn = p2(th0, th1) * p2s(scale);
+      const P2 sn = acos2(k3) * p2s(scale);
       int i0 = min((int)sn.v.x, ntheta - 1), i1 = min((int)sn.v.y, ntheta - 1);
       const P2 f = fma2(p2((float)i0, (float)i1), M1, sn);
       const float4 a0 = F[i0], b0 = F[i0 + 1], a1 = F[i1], b1 = F[i1 + 1];
@@ -835,6 +853,150 @@ __device__ void rt_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
       }
     }
   }
+}
+
+// ------------------------------------------------------------------ collect: CB, FP32x2
+// Frame products of one event, splat for packed arithmetic.
+struct F2Frame {
+  P2 ctcp, ctsp, nst, nsp, cp, stcp, stsp, ct, sp, ncp, nstcp, nstsp;
+};
+__device__ __forceinline__ F2Frame frame2(float ct, float st, float cp, float sp) {
+  return F2Frame{p2s(ct * cp), p2s(ct * sp), p2s(-st),      p2s(-sp),      p2s(cp),       p2s(st * cp),
+                 p2s(st * sp), p2s(ct),      p2s(sp),       p2s(-cp),      p2s(-st * cp), p2s(-st * sp)};
+}
+
+// update_E (src/utils.jl:170-192) for two outgoing directions at once: the field E and
+// the frame are the event's; k and its basis Eh are the two bins'.
+template <bool MIE>
+__device__ __forceinline__ void update_E2(const F2Frame& F, const float E[4], P2 kx, P2 ky, P2 kz, P2 ehx,
+                                          P2 ehy, const float4* S, int ntheta, float scale, P2 out[4]) {
+  const P2 M1 = p2s(-1.0f);
+  const P2 rx = fma2(kx, F.ctcp, fma2(ky, F.ctsp, kz * F.nst));
+  const P2 ry = fma2(kx, F.nsp, ky * F.cp);
+  const P2 rz = fma2(kx, F.stcp, fma2(ky, F.stsp, kz * F.ct));
+  P2 s2 = fma2(rx, rx, ry * ry);
+  const bool pole0 = s2.v.x < 1e-24f, pole1 = s2.v.y < 1e-24f;
+  s2.v.x = fmaxf(s2.v.x, 1e-30f);
+  s2.v.y = fmaxf(s2.v.y, 1e-30f);
+  const P2 r = p2(rsqrt_approx(s2.v.x), rsqrt_approx(s2.v.y));
+  P2 kcp = rx * r, ksp = ry * r, kst = s2 * r, kct = rz;
+  // spherical_from_cartesian's pole branch (src/utils.jl:12-14)
+  if (pole0) {
+    kcp.v.x = 1.f;
+    ksp.v.x = 0.f;
+    kst.v.x = 0.f;
+    kct.v.x = rz.v.x > 0.f ? 1.f : (rz.v.x < 0.f ? -1.f : 0.f);
+  }
+  if (pole1) {
+    kcp.v.y = 1.f;
+    ksp.v.y = 0.f;
+    kst.v.y = 0.f;
+    kct.v.y = rz.v.y > 0.f ? 1.f : (rz.v.y < 0.f ? -1.f : 0.f);
+  }
+  const P2 hx = fma2(ksp, F.ctcp, kcp * F.sp);
+  const P2 hy = fma2(ksp, F.ctsp, kcp * F.ncp);
+  const P2 kk = kct * kcp, ks = kct * ksp;
+  const P2 vx = fma2(kk, F.ctcp, fma2(ks, F.nsp, kst * F.nstcp));
+  const P2 vy = fma2(kk, F.ctsp, fma2(ks, F.cp, kst * F.nstsp));
+  const P2 cpsi = fma2(ehx, hx, ehy * hy);
+  const P2 spsi = fma2(ehx, vx, ehy * vy);
+  const P2 SE0 = p2s(E[0]), SE1 = p2s(E[1]), SE2 = p2s(E[2]), SE3 = p2s(E[3]);
+  const P2 ar = fma2(SE0, kcp, SE2 * ksp), ai = fma2(SE1, kcp, SE3 * ksp);
+  const P2 br = fma2(p2s(-E[0]), ksp, SE2 * kcp), bi = fma2(p2s(-E[1]), ksp, SE3 * kcp);
+  P2 sar, sai, sbr, sbi;
+  if (MIE) {
+    const P2 sn = acos2(rz) * p2s(scale);
+    const int i0 = min((int)sn.v.x, ntheta - 1), i1 = min((int)sn.v.y, ntheta - 1);
+    const P2 f = fma2(p2((float)i0, (float)i1), M1, sn);
+    const P2 w0 = fma2(f, M1, p2s(2.0f)), w1 = f + M1;  // the (2 - f, f - 1) weights of mie.jl:80-85
+    const float4 a0 = S[i0], b0 = S[i0 + 1], a1 = S[i1], b1 = S[i1 + 1];
+    const P2 s1r = fma2(w0, p2(a0.x, a1.x), w1 * p2(b0.x, b1.x));
+    const P2 s1i = fma2(w0, p2(a0.y, a1.y), w1 * p2(b0.y, b1.y));
+    const P2 s2r = fma2(w0, p2(a0.z, a1.z), w1 * p2(b0.z, b1.z));
+    const P2 s2i = fma2(w0, p2(a0.w, a1.w), w1 * p2(b0.w, b1.w));
+    const P2 nai = ai * M1, nbi = bi * M1;
+    sar = fma2(s1r, ar, s1i * nai);
+    sai = fma2(s1r, ai, s1i * ar);
+    sbr = fma2(s2r, br, s2i * nbi);
+    sbi = fma2(s2r, bi, s2i * br);
+  } else {  // S = diag(i, i cos)
+    sar = ai * M1;
+    sai = ar;
+    sbr = (bi * rz) * M1;
+    sbi = br * rz;
+  }
+  out[0] = fma2(sar, cpsi, sbr * spsi);
+  out[1] = fma2(sai, cpsi, sbi * spsi);
+  out[2] = fma2(sbr, cpsi, (sar * spsi) * M1);
+  out[3] = fma2(sbi, cpsi, (sai * spsi) * M1);
+}
+
+struct CBLaneF2 {
+  P2 kx, ky, kz, ehx, ehy, g, cf, sf, c1, c2, c3;
+  bool upb0, upb1;
+  P2 acc[4];
+  P2 lad;
+};
+
+// The reciprocal-path CB bins of src/gpu.jl:90-140 for one event, two bins per lane.
+template <bool MIE, bool SPHERE>
+__device__ __forceinline__ float cbn_event_f2(CBLaneF2& C, const EventP<float>& E, const DevScatterer& s1,
+                                              float tau0l, bool peak_lane) {
+  const F2Frame FA = frame2(E.fct, E.fst, E.fcp, E.fsp);
+  const F2Frame FB = frame2(E.bct, E.bst, E.bcp, E.bsp);
+  const float scale = table_scale<float>(s1);
+  const P2 M1 = p2s(-1.0f);
+  P2 ea[4], eb[4];
+  update_E2<MIE>(FA, E.ea, C.kx, C.ky, C.kz, C.ehx, C.ehy, s1.S, s1.ntheta, scale, ea);
+  update_E2<MIE>(FB, E.eb, C.kx, C.ky, C.kz, C.ehx, C.ehy, s1.S, s1.ntheta, scale, eb);
+  // Phase kl (ki + kf).(xa - xb) in turns, cancellation-free in the backscatter frame.
+  const P2 turns = fma2(C.c1, p2s(E.v1), fma2(C.c2, p2s(E.v2), C.c3 * p2s(E.v3)));
+  float sn0, cs0, sn1, cs1;
+  MT<float>::sincos_turns(turns.v.x - rintf(turns.v.x), &sn0, &cs0);
+  MT<float>::sincos_turns(turns.v.y - rintf(turns.v.y), &sn1, &cs1);
+  const P2 sn = p2(sn0, sn1), cs = p2(cs0, cs1), nsn = p2(-sn0, -sn1);
+  P2 ta2, tb2;
+  if (SPHERE) {
+    const P2 kxa = fma2(C.kx, p2s(E.xax), fma2(C.ky, p2s(E.xay), C.kz * p2s(E.xaz)));
+    const P2 kxb = fma2(C.kx, p2s(E.xbx), fma2(C.ky, p2s(E.xby), C.kz * p2s(E.xbz)));
+    ta2 = p2(sphere_t(kxa.v.x, E.Da), sphere_t(kxa.v.y, E.Da)) * p2s((float)LOG2E_D);
+    tb2 = p2(sphere_t(kxb.v.x, E.Db), sphere_t(kxb.v.y, E.Db)) * p2s((float)LOG2E_D);
+  } else {
+    ta2 = p2(C.upb0 ? E.a_up : E.a_dn, C.upb1 ? E.a_up : E.a_dn) * C.g;
+    tb2 = p2(C.upb0 ? E.b_up : E.b_dn, C.upb1 ? E.b_up : E.b_dn) * C.g;
+  }
+  tb2 = tb2 + p2s(E.tab2);
+  const bool ma0 = ta2.v.x <= tau0l, ma1 = ta2.v.y <= tau0l;
+  const P2 na = p2(ma0 ? MT<float>::exp2n(0.5f * ta2.v.x) : 0.f, ma1 ? MT<float>::exp2n(0.5f * ta2.v.y) : 0.f);
+  const P2 nb = p2(fabsf(tb2.v.x) <= tau0l ? MT<float>::exp2n(0.5f * tb2.v.x) : 0.f,
+                   fabsf(tb2.v.y) <= tau0l ? MT<float>::exp2n(0.5f * tb2.v.y) : 0.f);
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    ea[s] = ea[s] * na;
+    eb[s] = eb[s] * nb;
+  }
+  const P2 Ia = fma2(ea[0], ea[0], fma2(ea[1], ea[1], fma2(ea[2], ea[2], ea[3] * ea[3])));
+  const P2 Ib = fma2(eb[0], eb[0], fma2(eb[1], eb[1], fma2(eb[2], eb[2], eb[3] * eb[3])));
+  const P2 c1r = fma2(ea[0], cs, fma2(ea[1], nsn, eb[0])), c1i = fma2(ea[0], sn, fma2(ea[1], cs, eb[1]));
+  const P2 c2r = fma2(ea[2], cs, fma2(ea[3], nsn, eb[2])), c2i = fma2(ea[2], sn, fma2(ea[3], cs, eb[3]));
+  const P2 qh = fma2(c1r, c1r, c1i * c1i), qv = fma2(c2r, c2r, c2i * c2i);
+  P2 S0 = qh + qv, S1 = fma2(qh, M1, qv);
+  P2 S2 = fma2(c2r, c1r, c2i * c1i) * p2s(2.0f);
+  P2 S3 = fma2(c2i, c1r, (c2r * c1i) * M1) * p2s(-2.0f);
+  const P2 den = Ia + Ib;
+  const P2 scl = p2(den.v.x > 0.f ? __fdividef(Ia.v.x, den.v.x) : 0.f,
+                    den.v.y > 0.f ? __fdividef(Ia.v.y, den.v.y) : 0.f);
+  S0 = S0 * scl;
+  S1 = S1 * scl;
+  S2 = S2 * scl;
+  S3 = S3 * scl;
+  const P2 R1 = fma2(C.cf, S1, C.sf * S2), R2 = fma2(C.cf, S2, (C.sf * S1) * M1);
+  C.acc[0] = C.acc[0] + S0;
+  C.acc[1] = C.acc[1] + R1;
+  C.acc[2] = C.acc[2] + R2;
+  C.acc[3] = C.acc[3] + S3;
+  C.lad = C.lad + Ia;
+  return peak_lane ? S0.v.x : 0.f;
 }
 
 // ------------------------------------------------------------------ collect: CB tile
@@ -1011,6 +1173,107 @@ __device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int 
   }
 }
 
+// ------------------------------------------------------------------ collect: CB tile, FP32x2 lanes
+template <int BS>
+__device__ void cb_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int tile, int pc, int q0, int q1) {
+  constexpr int NB = 2;
+  const int lane = threadIdx.x & 31;
+  const int ngrp = (B.nthetab + NB - 1) / NB;
+  const int item = tile * 32 + lane;
+  const bool lane_ok = item < ngrp * B.nphib;
+  const int it = lane_ok ? item : 0;
+  const int j2 = it % B.nphib, grp = it / B.nphib;
+  int bb[NB];
+  bool okb[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    const int j1 = grp * NB + i;
+    okb[i] = lane_ok && j1 < B.nthetab;
+    bb[i] = okb[i] ? j2 * B.nthetab + j1 : 0;
+  }
+  CBLaneF2 C;
+  C.kx = p2(B.kfx[bb[0]], B.kfx[bb[1]]);
+  C.ky = p2(B.kfy[bb[0]], B.kfy[bb[1]]);
+  C.kz = p2(B.kfz[bb[0]], B.kfz[bb[1]]);
+  C.ehx = p2(B.ehx[bb[0]], B.ehx[bb[1]]);
+  C.ehy = p2(B.ehy[bb[0]], B.ehy[bb[1]]);
+  C.g = p2(B.gb[bb[0]], B.gb[bb[1]]);
+  C.cf = p2(B.cf2[bb[0]], B.cf2[bb[1]]);
+  C.sf = p2(B.sf2[bb[0]], B.sf2[bb[1]]);
+  C.c1 = p2(B.c1[bb[0]], B.c1[bb[1]]);
+  C.c2 = p2(B.c2[bb[0]], B.c2[bb[1]]);
+  C.c3 = p2(B.c3[bb[0]], B.c3[bb[1]]);
+  C.upb0 = B.upb[bb[0]] != 0;
+  C.upb1 = B.upb[bb[1]] != 0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) C.acc[s] = p2s(0.f);
+  C.lad = p2s(0.f);
+  const bool peak_lane = lane_ok && j2 == 0 && grp == 0;
+  const DevInstance& in = sh.inst;
+  const DevScatterer& s1 = in.scat[in.layers[0].scat];
+  const float tau0l = (float)(in.tau0 * LOG2E_D);
+  const bool sphere = in.geom == 1, mie = s1.kind == 1;
+  const int nn = sh.cnt[pc][2];
+  for (int q = q0; q < min(q1, nn); ++q) {
+    const int e = sh.list[2][q];
+    const EventP<float>& E = sh.ev[e];
+    float pk;
+    if (mie)
+      pk = sphere ? cbn_event_f2<true, true>(C, E, s1, tau0l, peak_lane)
+                  : cbn_event_f2<true, false>(C, E, s1, tau0l, peak_lane);
+    else
+      pk = sphere ? cbn_event_f2<false, true>(C, E, s1, tau0l, peak_lane)
+                  : cbn_event_f2<false, false>(C, E, s1, tau0l, peak_lane);
+    if (peak_lane) sh.peak[e] = pk;
+  }
+  // Order-1 events (a few per path) use the scalar single-scattering bins.
+  if (max(q0, nn) < q1) {
+    CBLane<float, NB> Cs;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int b = bb[i];
+      Cs.kx[i] = B.kfx[b];
+      Cs.ky[i] = B.kfy[b];
+      Cs.kz[i] = B.kfz[b];
+      Cs.ehx[i] = B.ehx[b];
+      Cs.ehy[i] = B.ehy[b];
+      Cs.g[i] = B.gb[b];
+      Cs.cf[i] = B.cf2[b];
+      Cs.sf[i] = B.sf2[b];
+      Cs.upb[i] = B.upb[b] != 0;
+#pragma unroll
+      for (int s = 0; s < 4; ++s) Cs.acc[i][s] = 0.f;
+      Cs.lad[i] = 0.f;
+    }
+    for (int q = max(q0, nn); q < q1; ++q) {
+      const int e = sh.list[3][q - nn];
+      const EventP<float>& E = sh.ev[e];
+      float pk;
+      if (mie)
+        pk = sphere ? cb1_event<float, NB, true, true>(Cs, E, s1, tau0l, peak_lane)
+                    : cb1_event<float, NB, true, false>(Cs, E, s1, tau0l, peak_lane);
+      else
+        pk = sphere ? cb1_event<float, NB, false, true>(Cs, E, s1, tau0l, peak_lane)
+                    : cb1_event<float, NB, false, false>(Cs, E, s1, tau0l, peak_lane);
+      if (peak_lane) sh.peak[e] = pk;
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) C.acc[s] = C.acc[s] + p2(Cs.acc[0][s], Cs.acc[1][s]);
+    C.lad = C.lad + p2(Cs.lad[0], Cs.lad[1]);
+  }
+  if (lane_ok) {
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      if (okb[i]) {
+        double* dst = in.Icb + 4 * (size_t)bb[i];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) atomicAdd(dst + s, (double)(i ? C.acc[s].v.y : C.acc[s].v.x));
+        atomicAdd(in.ladder + bb[i], (double)(i ? C.lad.v.y : C.lad.v.x));
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ the kernel
 template <typename T, int BS, int NBR, int NBC, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
@@ -1130,7 +1393,10 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
         if (w >= total) break;
         if (w < icb) {
           const int c = w % ccb;
-          cb_tile<T, NBC, BS>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
+          if constexpr (std::is_same<T, float>::value && NBC == 2)
+            cb_tile_f2<BS>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
+          else
+            cb_tile<T, NBC, BS>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
         } else if (w < icb + iup) {
           w -= icb;
           const int c = w % cup;

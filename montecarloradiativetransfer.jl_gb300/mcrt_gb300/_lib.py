@@ -59,6 +59,7 @@ class RunOpts(C.Structure):
         ("precision", C.c_int), ("kernel", C.c_int), ("seed", C.c_uint64),
         ("instance", C.c_uint32), ("rng_mode", C.c_int), ("photon_begin", C.c_int64),
         ("block_size", C.c_int), ("blocks_per_sm", C.c_int), ("plain_threads", C.c_int),
+        ("table_staging", C.c_int),
     ]
 
 
@@ -69,6 +70,25 @@ class Stats(C.Structure):
         ("cb1_evals", C.c_double), ("cbn_evals", C.c_double), ("kernel_ms", C.c_double),
         ("status_flags", C.c_int), ("block_size", C.c_int), ("blocks", C.c_int),
     ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("memory_cap_bytes", C.c_double), ("max_active", C.c_int), ("wave_photons", C.c_int64),
+                ("min_quantum", C.c_int64), ("precision", C.c_int), ("use_graphs", C.c_int)]
+
+
+class RequestC(C.Structure):
+    _fields_ = [("config", C.POINTER(ConfigC)), ("geometry", C.POINTER(GeometryC)), ("I0", C.c_double * 4),
+                ("seed", C.c_uint64), ("instance", C.c_uint32), ("n_photons", C.c_int64)]
+
+
+class TicketInfo(C.Structure):
+    _fields_ = [("submitted_s", C.c_double), ("admitted_s", C.c_double), ("completed_s", C.c_double),
+                ("footprint_bytes", C.c_double), ("photons", C.c_int64), ("waves", C.c_int),
+                ("status_flags", C.c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -107,6 +127,12 @@ SIGNATURES = {
     "mcrt_measure_fp32_peak": [_VP, _dp],
     "mcrt_simulate_noalloc": [_VP, C.POINTER(ConfigC), C.POINTER(GeometryC), _dp, C.POINTER(RunOpts),
                               _dp, _dp, _dp, _dp, C.POINTER(Stats)],
+    "mcrt_server_create": [_VP, C.POINTER(ServerOpts), C.POINTER(_VP)],
+    "mcrt_server_submit": [_VP, C.POINTER(RequestC), C.POINTER(C.c_uint64)],
+    "mcrt_server_wait": [_VP, C.c_uint64, C.c_double],
+    "mcrt_server_result": [_VP, C.c_uint64, _dp, _dp, _dp, _dp, C.POINTER(TicketInfo)],
+    "mcrt_server_stats": [_VP, _dp],
+    "mcrt_server_destroy": [_VP],
 }
 
 _lib = None

@@ -97,10 +97,16 @@ def default_context() -> Context:
     return _default
 
 
+_STAGING = {"auto": 0, "shared": 1, "global": 2}
+
+
 def run_opts(precision="fp32", kernel="persistent", seed=1, instance=0, rng_mode=0, photon_begin=0,
-             block_size=0, blocks_per_sm=0, plain_threads=0) -> _lib.RunOpts:
+             block_size=0, blocks_per_sm=0, plain_threads=0, table_staging="auto") -> _lib.RunOpts:
+    """Launch options (mcrt_run_opts). Zero block_size / blocks_per_sm and "auto" staging
+    leave the choice to the library's autotuner."""
     return _lib.RunOpts(_PREC[precision], _KERN[kernel], int(seed), int(instance), int(rng_mode),
-                        int(photon_begin), int(block_size), int(blocks_per_sm), int(plain_threads))
+                        int(photon_begin), int(block_size), int(blocks_per_sm), int(plain_threads),
+                        _STAGING[table_staging])
 
 
 def _views(cfg, Irt, Icb, lad):
@@ -244,6 +250,76 @@ class Batch:
     def close(self) -> None:
         if self.h:
             lib().mcrt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The continuous-batching request loop of libmcrt (mcrt_server_*).
+
+    ``submit`` queues a simulate() request and returns a ticket; ``result`` waits for it
+    and returns ``(A, Irt, Icb, ladder, info)`` divided by the request's photon count,
+    where ``info`` holds the submit / admit / completion times and the waves it took."""
+
+    def __init__(self, *, ctx: Optional[Context] = None, memory_cap_bytes: float = 20e9, max_active: int = 256,
+                 wave_photons: int = 1 << 20, min_quantum: int = 4096, precision: str = "fp32",
+                 use_graphs: bool = True):
+        self.ctx = ctx or default_context()
+        o = _lib.ServerOpts(float(memory_cap_bytes), int(max_active), int(wave_photons), int(min_quantum),
+                            _PREC[precision], int(use_graphs))
+        h = C.c_void_p()
+        check(lib().mcrt_server_create(self.ctx.h, C.byref(o), C.byref(h)))
+        self.h = h
+        self._shapes = {}
+
+    def submit(self, cfg, g, I0, n_photons: int, seed: int = 1, instance: int = 0) -> int:
+        g.validate()
+        cc = cfg.to_c()
+        gc, keep = self.ctx.geometry_c(g)
+        r = _lib.RequestC(C.pointer(cc), C.pointer(gc), (C.c_double * 4)(*[float(v) for v in I0]), int(seed),
+                          int(instance), int(n_photons))
+        t = C.c_uint64()
+        check(lib().mcrt_server_submit(self.h, C.byref(r), C.byref(t)))  # the server copies the request
+        self._shapes[t.value] = (cfg.Ntheta, cfg.Nphi, cfg.Nthetab, cfg.Nphib)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: float = 1e9) -> bool:
+        rc = lib().mcrt_server_wait(self.h, int(ticket), float(timeout_ms))
+        if rc == _lib.MCRT_ETIMEDOUT:
+            return False
+        check(rc)
+        return True
+
+    def result(self, ticket: int, timeout_ms: float = 1e9):
+        if not self.wait(ticket, timeout_ms):
+            raise TimeoutError(f"ticket {ticket} not done within {timeout_ms} ms")
+        nt, nph, ntb, npb = self._shapes.pop(ticket)
+        A = np.zeros(5)
+        Irt = np.zeros(4 * nt * nph)
+        Icb = np.zeros(4 * ntb * npb)
+        lad = np.zeros(ntb * npb)
+        info = _lib.TicketInfo()
+        check(lib().mcrt_server_result(self.h, int(ticket), dptr(A), dptr(Irt), dptr(Icb), dptr(lad),
+                                       C.byref(info)))
+        irt = Irt.reshape(nph, nt, 4).transpose(2, 1, 0)
+        icb = Icb.reshape(npb, ntb, 4).transpose(2, 1, 0)
+        return A, irt, icb, lad.reshape(npb, ntb).T, info.as_dict()
+
+    def stats(self) -> dict:
+        v = np.zeros(8)
+        check(lib().mcrt_server_stats(self.h, dptr(v)))
+        keys = ["completed", "photons", "waves", "busy_s", "peak_resident_bytes", "resident_bytes", "pending",
+                "active"]
+        return dict(zip(keys, v.tolist()))
+
+    def close(self) -> None:
+        if self.h:
+            lib().mcrt_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -1,0 +1,107 @@
+"""The continuous-batching server (mcrt_server_*): results equal simulate(), a request's
+result is the same alone and in a mix, admission respects the memory cap, and graph
+replay equals direct launches."""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import scaled_err
+
+pytestmark = pytest.mark.gpu
+N0 = [1.0, 0.0, 0.0, 0.0]
+
+
+def small_cfg(M, g):
+    return M.Config(g, number_of_rays=1, Ntheta=16, Nphi=8, Nphib=4, thetab=np.deg2rad(np.linspace(0, 3, 12)),
+                    maximum_scattering_times=400)
+
+
+def requests(M, mie5, mie2):
+    ray = M.RayleighScatterer(0.97, 100.0)
+    out = []
+    for i in range(12):
+        if i % 3 == 0:
+            g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=(0.5 + i) * ray.kl, scatterer=ray)])
+        elif i % 3 == 1:
+            g = M.PlaneGeometry(math.radians(140 + i), 0.2 * i, [M.Layer(d=(0.3 + 0.2 * i) * mie5.kl, scatterer=mie5)])
+        else:
+            g = M.SphereGeometry(R=(1 + 0.3 * i) * mie2.kl, scatterer=mie2)
+        I = [N0, [1, 1, 0, 0], [1, 0, 0, -1]][i % 3]
+        out.append((small_cfg(M, g), g, I, 200 + 377 * i, 100 + i, i))
+    return out
+
+
+def compare(a, b, tol):
+    assert scaled_err(a[0], b[0]) < tol
+    assert scaled_err(a[1], b[1]) < tol
+    assert scaled_err(a[2], b[2]) < tol
+
+
+def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2):
+    reqs = requests(M, mie5, mie2)[:6]
+    srv = M.Server(precision="fp64", wave_photons=2048, min_quantum=256)
+    tickets = [srv.submit(c, g, I, n, seed=s, instance=i) for c, g, I, n, s, i in reqs]
+    for t, (c, g, I, n, s, i) in zip(tickets, reqs):
+        A, Irt, Icb, lad, info = srv.result(t)
+        solo = M.simulate(c.replace(number_of_rays=n), g, I, precision="fp64", seed=s, instance=i)
+        compare((A, Irt, Icb), (np.array(solo[:5]), solo[5], solo[6]), 1e-9)
+        assert info["photons"] == n and info["waves"] >= 1
+        assert info["submitted_s"] <= info["admitted_s"] <= info["completed_s"]
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["resident_bytes"] == 0
+    srv.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
+def test_result_is_the_same_alone_and_in_the_mix(M, gpu_ctx, mie5, mie2, prec, tol):
+    reqs = requests(M, mie5, mie2)
+    x = reqs[4]
+    srv = M.Server(precision=prec, wave_photons=4096, min_quantum=512)
+    c, g, I, n, s, i = x
+    alone = srv.result(srv.submit(c, g, I, 4 * n, seed=s, instance=i))
+    tickets = []
+    for k, (c2, g2, I2, n2, s2, i2) in enumerate(reqs):
+        if k == 4:
+            tickets.append(srv.submit(c, g, I, 4 * n, seed=s, instance=i))
+        else:
+            tickets.append(srv.submit(c2, g2, I2, n2, seed=s2, instance=i2))
+    mixed = srv.result(tickets[4])
+    for k, t in enumerate(tickets):
+        if k != 4:
+            srv.result(t)
+    compare(mixed[:3], alone[:3], tol)
+    assert mixed[4]["waves"] >= 2  # its photons were spread over waves shared with others
+    srv.close()
+
+
+def test_admission_respects_the_memory_cap_and_waits_time_out(M, gpu_ctx, mie5, mie2):
+    reqs = requests(M, mie5, mie2)
+    srv0 = M.Server(precision="fp32")
+    t0 = srv0.submit(*reqs[0][:4])
+    fp = srv0.result(t0)[4]["footprint_bytes"]
+    srv0.close()
+    cap = 2.5 * fp
+    srv = M.Server(precision="fp32", memory_cap_bytes=cap, wave_photons=2048, min_quantum=256)
+    ts = [srv.submit(c, g, I, n, seed=s, instance=i) for c, g, I, n, s, i in reqs[:6:3] * 3]
+    big = srv.submit(*reqs[0][:3], 200000)
+    assert srv.wait(big, 0.001) is False  # still queued or running
+    for t in ts:
+        srv.result(t)
+    srv.result(big)
+    st = srv.stats()
+    assert st["peak_resident_bytes"] <= cap
+    assert st["completed"] == len(ts) + 1
+    srv.close()
+
+
+def test_graph_replay_matches_direct_launches(M, gpu_ctx, mie5, mie2):
+    reqs = requests(M, mie5, mie2)[1:4]
+    outs = []
+    for graphs in (True, False):
+        srv = M.Server(precision="fp64", use_graphs=graphs, wave_photons=2048, min_quantum=256)
+        ts = [srv.submit(c, g, I, n, seed=s, instance=i) for c, g, I, n, s, i in reqs]
+        outs.append([srv.result(t) for t in ts])
+        srv.close()
+    for a, b in zip(*outs):
+        compare(a[:3], b[:3], 1e-9)
