@@ -166,6 +166,39 @@ def serve_leg(M, ctx, n_req, scale, rate_hz=200.0, seed=5):
             "memory_cap_bytes": 20e9}
 
 
+def batch_leg(M, ctx, n_inst=256, scale=1e-3, seed=4):
+    """One persistent launch over uneven slab instances drawn like the 256-instance batch
+    (optical thickness log-uniform in [0.1, 50], albedo uniform in [0.5, 0.9999], Rayleigh
+    or Mie with x in U[0.5, 10], n in U[1.3, 1.6], k log-uniform in [1e-5, 1e-2] on 1801
+    angles, photon budgets lognormal(median 1e7, sigma 1)) with the budgets multiplied by
+    `scale`."""
+    rng = np.random.default_rng(seed)
+    insts = []
+    ray_cache = None
+    for i in range(n_inst):
+        if rng.random() < 0.5:
+            sc = M.RayleighScatterer(1.0, 1.0)
+        else:
+            x = rng.uniform(0.5, 10.0)
+            m = complex(rng.uniform(1.3, 1.6), 10 ** rng.uniform(-5, -2))
+            sc = M.MieScatterer(x / (2 * math.pi), m, 1.0, 0.1, Ntheta=1801)
+        tau = 10 ** rng.uniform(-1, math.log10(50))
+        omega = rng.uniform(0.5, 0.9999)
+        g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=tau * sc.kl, scatterer=sc, omega=omega)])
+        n = max(1, int(rng.lognormal(math.log(1e7), 1.0) * scale))
+        insts.append({"geometry": g, "I0": [1.0, 0.0, 0.0, 0.0], "n_photons": n, "seed": seed, "instance": i})
+        ray_cache = ray_cache or g
+    cfg = M.Config(ray_cache, number_of_rays=1)
+    b = M.Batch(cfg, insts, ctx=ctx, precision="fp32")
+    b.launch()
+    ms, photons = b.timing()
+    b.launch()
+    ms, photons = b.timing()
+    b.close()
+    return {"instances": n_inst, "budget_scale": scale, "photons": photons, "kernel_ms": ms,
+            "paths_per_s": photons / (ms / 1e3)}
+
+
 def cpu_oracle_rate(M, n_sample, threads=0):
     """Times the oracle (the FP64 C++ restatement of the reference's CPU path) on a bounded
     sample of the same workload with all host threads."""
@@ -345,8 +378,10 @@ def main():
         vplain = n64 / (rp["stats"]["kernel_ms"] / 1e3)
         cpu_v, cores, cpu_dt = cpu_oracle_rate(M, args.cpu_sample)
         serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
+        batch = batch_leg(M, ctx)
         extras = {
             "serve": serve,
+            "batch_uneven_slabs": batch,
             "fp64_persistent": {"value": v64, "unit": "paths/s", "sample_photons": np64},
             "fp64_plain": {"value": vplain, "unit": "paths/s", "sample_photons": n64,
                            "threads": plain_threads},
