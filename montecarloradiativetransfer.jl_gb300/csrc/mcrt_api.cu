@@ -241,6 +241,25 @@ namespace {
 
 constexpr double PI = host::PI;
 
+// Tally doubles of one instance: Irt | Icb | ladder | acc (NACC) | Fourier RT coefficients.
+struct TallyLayout {
+  size_t nrt, ncb, per_inst;
+};
+TallyLayout tally_layout(const mcrt_config* c) {
+  TallyLayout t;
+  t.nrt = 4 * (size_t)c->n_theta * c->n_phi;
+  t.ncb = 4 * (size_t)c->n_theta_b * c->n_phi_b;
+  t.per_inst = t.nrt + t.ncb + t.ncb / 4 + NACC + 20 * (size_t)c->n_theta;
+  return t;
+}
+void assign_tally(DevInstance& D, double* t, const TallyLayout& L) {
+  D.Irt = t;
+  D.Icb = t + L.nrt;
+  D.ladder = t + L.nrt + L.ncb;
+  D.acc = D.ladder + L.ncb / 4;
+  D.Frt = D.acc + NACC;
+}
+
 int validate_config(const mcrt_config* c, int geom) {
   if (!c) return set_err(MCRT_EINVAL, "config is NULL");
   if (c->number_of_rays < 0) return set_err(MCRT_EINVAL, "number_of_rays must be >= 0");
@@ -496,6 +515,11 @@ int make_instance(const mcrt_config* c, const mcrt_geometry* g, const double I0[
   D.key0 = (unsigned)seed;
   D.key1 = (unsigned)(seed >> 32) + 0x632BE5ABu * instance;
   D.rng_mode = rng_mode;
+  // Rayleigh peel-off in a slab: the bin's Stokes vector is a degree-2 trigonometric
+  // polynomial in its azimuth and its attenuation depends on the polar angle only.
+  bool all_rayleigh = true;
+  for (int s = 0; s < D.n_scat; ++s) all_rayleigh = all_rayleigh && D.scat[s].kind == 0;
+  D.rt_fourier = (g->kind == MCRT_PLANE && all_rayleigh && c->n_phi >= 5) ? 1 : 0;
   return MCRT_OK;
 }
 
@@ -655,19 +679,16 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
     }
     G.hinst[i].bins = it->second;
   }
-  G.nrt = 4 * (size_t)c->n_theta * c->n_phi;
-  G.ncb = 4 * (size_t)c->n_theta_b * c->n_phi_b;
-  G.per_inst = G.nrt + G.ncb + G.ncb / 4 + NACC;
+  const TallyLayout TL = tally_layout(c);
+  G.nrt = TL.nrt;
+  G.ncb = TL.ncb;
+  G.per_inst = TL.per_inst;
   CK(G.d_tally.alloc(G.per_inst * n * sizeof(double)));
-  CK(G.d_claim.alloc(n * sizeof(unsigned long long)));
+  CK(G.d_claim.alloc(2 * n * sizeof(unsigned long long)));
   CK(G.d_status.alloc(sizeof(unsigned)));
   for (int i = 0; i < n; ++i) {
-    double* base = G.d_tally.as<double>() + G.per_inst * i;
-    G.hinst[i].Irt = base;
-    G.hinst[i].Icb = base + G.nrt;
-    G.hinst[i].ladder = base + G.nrt + G.ncb;
-    G.hinst[i].acc = base + G.nrt + G.ncb + G.ncb / 4;
-    G.hinst[i].claim = G.d_claim.as<unsigned long long>() + i;
+    assign_tally(G.hinst[i], G.d_tally.as<double>() + G.per_inst * i, TL);
+    G.hinst[i].claim = G.d_claim.as<unsigned long long>() + 2 * i;
   }
   std::vector<DevInstance> dev(n);
   for (int s = 0; s < n; ++s) dev[s] = G.hinst[G.order[s]];
@@ -1128,12 +1149,8 @@ int srv_admit(mcrt_server* S) {
                                               : pack_bins_at<double>(H, (unsigned char*)r->bins.p);
     CK(cudaMemcpyAsync(r->bins.p, r->binbytes.data(), r->binbytes.size(), cudaMemcpyHostToDevice, S->stream));
     CK(cudaMemsetAsync(r->tally.p, 0, r->per_inst * sizeof(double), S->stream));
-    double* t = (double*)r->tally.p;
     r->D.bins = r->bins.p;
-    r->D.Irt = t;
-    r->D.Icb = t + r->nrt;
-    r->D.ladder = t + r->nrt + r->ncb;
-    r->D.acc = t + r->nrt + r->ncb + r->ncb / 4;
+    assign_tally(r->D, (double*)r->tally.p, tally_layout(&r->cfg));
     r->state = 1;
     r->t_adm = now_s();
     S->active.push_back(r);
@@ -1232,7 +1249,7 @@ int srv_build_wave(mcrt_server* S, int b, bool& launched) {
     } else {
       W.n_photons = 0;  // padding: skipped by the kernel
     }
-    W.claim = sl.d_claim.as<unsigned long long>() + i;
+    W.claim = sl.d_claim.as<unsigned long long>() + 2 * i;
   }
   sl.members = members;
   sl.wave_id = wid;
@@ -1320,13 +1337,13 @@ extern "C" int mcrt_server_create(mcrt_ctx* ctx, const mcrt_server_opts* opts, m
   const size_t slots = (size_t)S->blocks * S->bs;
   for (auto& sl : S->slot) {
     CK(sl.d_wave.alloc(S->o.max_active * sizeof(DevInstance)));
-    CK(sl.d_claim.alloc(S->o.max_active * sizeof(unsigned long long)));
+    CK(sl.d_claim.alloc(2 * S->o.max_active * sizeof(unsigned long long)));
     CK(sl.d_status.alloc(sizeof(unsigned)));
     CK(sl.d_state.alloc(slots * S->ki.state_bytes));
     CK(sl.d_tacc.alloc(slots * NACC * sizeof(double)));
     CK(cudaMallocHost(&sl.h_wave, S->o.max_active * sizeof(DevInstance)));
     std::memset(sl.h_wave, 0, S->o.max_active * sizeof(DevInstance));
-    for (int i = 0; i < S->o.max_active; ++i) sl.h_wave[i].claim = sl.d_claim.as<unsigned long long>() + i;
+    for (int i = 0; i < S->o.max_active; ++i) sl.h_wave[i].claim = sl.d_claim.as<unsigned long long>() + 2 * i;
     CK(cudaEventCreate(&sl.start));
     CK(cudaEventCreate(&sl.done));
     if (S->o.use_graphs) {
@@ -1390,9 +1407,10 @@ extern "C" int mcrt_server_submit(mcrt_server* S, const mcrt_request* q, uint64_
   if (rc) return rc;
   HostBins H = make_bins(&r->cfg, r->geom.kind, kfs);
   r->binbytes = S->o.precision == MCRT_FP32 ? pack_bins_at<float>(H, nullptr) : pack_bins_at<double>(H, nullptr);
-  r->nrt = 4 * (size_t)c->n_theta * c->n_phi;
-  r->ncb = 4 * (size_t)c->n_theta_b * c->n_phi_b;
-  r->per_inst = r->nrt + r->ncb + r->ncb / 4 + NACC;
+  const TallyLayout TL = tally_layout(c);
+  r->nrt = TL.nrt;
+  r->ncb = TL.ncb;
+  r->per_inst = TL.per_inst;
   r->footprint = request_footprint(*r);
   if (r->footprint > S->o.memory_cap_bytes)
     return set_err(MCRT_EBUSY, "request footprint exceeds the server's memory cap");
@@ -1627,15 +1645,15 @@ extern "C" int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, cons
   const size_t slots = (size_t)blocks * bs;
 
   // Layout of the scratch array.
-  const size_t nrt = 4 * (size_t)cfg->n_theta * cfg->n_phi, ncb = 4 * (size_t)cfg->n_theta_b * cfg->n_phi_b;
-  const size_t per_inst = nrt + ncb + ncb / 4 + NACC;
+  const TallyLayout TL = tally_layout(cfg);
+  const size_t nrt = TL.nrt, ncb = TL.ncb, per_inst = TL.per_inst;
   std::vector<unsigned char> binbytes;
   const size_t off_inst = 0;
   const size_t off_bins = align256(sizeof(DevInstance));
   binbytes = prec == MCRT_FP32 ? pack_bins_at<float>(H, base + off_bins) : pack_bins_at<double>(H, base + off_bins);
   const size_t off_tally = align256(off_bins + binbytes.size());
   const size_t off_claim = align256(off_tally + per_inst * sizeof(double));
-  const size_t off_status = off_claim + sizeof(unsigned long long);
+  const size_t off_status = off_claim + 2 * sizeof(unsigned long long);
   const size_t off_state = align256(off_status + sizeof(unsigned));
   const size_t off_tacc = align256(off_state + slots * ki.state_bytes);
   const size_t need = off_tacc + slots * NACC * sizeof(double);
@@ -1649,10 +1667,7 @@ extern "C" int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, cons
   }
   double* tally = reinterpret_cast<double*>(base + off_tally);
   D.bins = base + off_bins;
-  D.Irt = tally;
-  D.Icb = tally + nrt;
-  D.ladder = tally + nrt + ncb;
-  D.acc = tally + nrt + ncb + ncb / 4;
+  assign_tally(D, tally, TL);
   D.claim = reinterpret_cast<unsigned long long*>(base + off_claim);
 
   // The array keeps the previous call's contents: write the inputs and clear the

@@ -83,13 +83,14 @@ struct __align__(16) DevInstance {
   long long nrays;         // number_of_rays (stratified test mode)
   unsigned key0, key1;
   int rng_mode;
-  int pad;
+  int rt_fourier;          // plane with Rayleigh scatterers only: RT bins by azimuthal Fourier modes
   const void* bins;        // BinTables<T> in device memory
   double* Irt;
   double* Icb;
   double* ladder;
   double* acc;             // NACC raw sums
-  unsigned long long* claim;  // photon claim counter of this instance
+  double* Frt;             // Fourier RT coefficients [ntheta][4 Stokes][5 modes] (rt_fourier)
+  unsigned long long* claim;  // [0] photons claimed, [1] photons finished by blocks, this launch
 };
 static_assert(sizeof(DevInstance) % 16 == 0, "DevInstance is copied as 16-byte words");
 

@@ -73,7 +73,8 @@ struct __align__(16) Shared {
   int item_next;
   int cur;
   int exhausted;
-  int pad;
+  int taken;   // photons of the current instance this block claimed in this launch
+  int expand;  // this block finished the instance's last photon (Fourier expansion)
 };
 
 struct KParams {
@@ -655,6 +656,160 @@ __device__ void rt_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool
         for (int s = 0; s < 4; ++s) atomicAdd(dst + s, (double)R.acc[i][s]);
       }
     }
+  }
+}
+
+// ------------------------------------------------------------------ collect: RT, Fourier modes
+// For Rayleigh scatterers the peel-off Stokes vector into a bin, expressed in the bin's
+// meridian frame, is a trigonometric polynomial of degree 2 in the bin azimuth
+// (dipole scattering is quadratic in the field), and in a slab the attenuation
+// inorm * exp(-t) depends on the polar bin only. So per (event, polar bin) the 5
+// Fourier coefficients of each Stokes component are taken from update_I at 5 equally
+// spaced azimuths (an exact 5-point DFT) and summed over events with the attenuation
+// weight. The block that finishes the launch's last photon of the instance expands the
+// coefficients into every configured azimuth (fourier_expand). This equals the per-bin
+// evaluation of src/gpu.jl:11-31 up to rounding and costs 5 evaluations per polar bin
+// instead of Nphi.
+
+// cos and sin of 2*pi*j/5 and of 4*pi*j/5, j = 0..4.
+template <typename T>
+__device__ __forceinline__ void fourier_node(int j, T& c1, T& s1, T& c2, T& s2) {
+  constexpr double C1 = 0.30901699437494742, S1 = 0.95105651629515357;   // 2*pi/5
+  constexpr double C2 = -0.80901699437494742, S2 = 0.58778525229247313;  // 4*pi/5
+  switch (j) {
+    case 0: c1 = T(1), s1 = T(0), c2 = T(1), s2 = T(0); break;
+    case 1: c1 = T(C1), s1 = T(S1), c2 = T(C2), s2 = T(S2); break;
+    case 2: c1 = T(C2), s1 = T(S2), c2 = T(C1), s2 = T(-S1); break;
+    case 3: c1 = T(C2), s1 = T(-S2), c2 = T(C1), s2 = T(S1); break;
+    default: c1 = T(C1), s1 = T(-S1), c2 = T(C2), s2 = T(-S2); break;
+  }
+}
+
+// Unweighted Rayleigh update_I into the direction (st cos(phib), st sin(phib), ct): the
+// arithmetic of rt_event with the Rayleigh phase matrix.
+template <typename T>
+__device__ __forceinline__ void rayleigh_peel(T st, T ct, T cb, T sb, const Frame<T>& f, const T I[4],
+                                              T o[4]) {
+  const T sDe = sb * f.cp - cb * f.sp, cD = cb * f.cp + sb * f.sp;
+  const T k1 = st * (f.ct * cD) - ct * f.st;
+  const T k2 = st * sDe;
+  const T k3 = st * (f.st * cD) + ct * f.ct;
+  T s2 = k1 * k1 + k2 * k2;
+  const bool pole = s2 < T(1e-24);
+  s2 = pole ? T(1) : s2;
+  const T r = MT<T>::rsqrt(s2);
+  const T cpk = pole ? T(1) : k1 * r, spk = pole ? T(0) : k2 * r, stk = pole ? T(0) : s2 * r;
+  const T ctk = pole ? (k3 > T(0) ? T(1) : (k3 < T(0) ? T(-1) : T(0))) : k3;
+  const T c2 = cpk * cpk - spk * spk, sr = T(-2) * spk * cpk;
+  const T q = c2 * I[1] + sr * I[2], u = -sr * I[1] + c2 * I[2];
+  const T bq = f.ct * sDe, c4 = f.st * sDe;
+  const T cpsi = spk * bq + cpk * cD;
+  const T spsi = ctk * (spk * cD - cpk * bq) + stk * c4;
+  const T c2p = cpsi * cpsi - spsi * spsi, s2p = T(2) * spsi * cpsi;
+  const T m2 = k3 * k3;
+  const T p11 = T(0.75) + T(0.75) * m2, p12 = T(-0.75) + T(0.75) * m2, p33 = T(1.5) * k3;
+  const T o1 = p12 * I[0] + p11 * q, o2 = p33 * u;
+  o[0] = p11 * I[0] + p12 * q;
+  o[1] = c2p * o1 + s2p * o2;
+  o[2] = -s2p * o1 + c2p * o2;
+  o[3] = p33 * I[3];
+}
+
+// One lane per polar bin of the hemisphere; events q0..q1 of the batch's list.
+template <typename T, int BS>
+__device__ void rt_fourier_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, bool upper, int q0,
+                                int q1) {
+  const int lane = threadIdx.x & 31;
+  const int r0 = upper ? B.up0 : B.lo0, r1 = upper ? B.up1 : B.lo1;
+  const int j1 = r0 + tile * 32 + lane;
+  const bool ok = j1 < r1;
+  const int jj = ok ? j1 : r0;
+  const T st = B.st[jj], ct = B.ct[jj], g = B.g[jj], w = ok ? B.w[jj] : T(0);
+  // sums over the configured azimuths of the 4 non-constant modes (for the escaped intensity)
+  T fs1 = T(0), fs2 = T(0), fs3 = T(0), fs4 = T(0);
+  for (int j2 = 0; j2 < B.nphi; ++j2) {
+    const T cp = B.cp[j2], sp = B.sp[j2];
+    fs1 += cp;
+    fs2 += sp;
+    fs3 += cp * cp - sp * sp;
+    fs4 += T(2) * sp * cp;
+  }
+  const T fs0 = T(B.nphi);
+  T acc[4][5];
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+#pragma unroll
+    for (int m = 0; m < 5; ++m) acc[s][m] = T(0);
+  const DevInstance& in = sh.inst;
+  const T tau0l = (T)(in.tau0 * LOG2E_D);
+  const int li = upper ? 0 : 1;
+  T* escarr = upper ? sh.esc_up : sh.esc_dn;
+  for (int q = q0; q < q1; ++q) {
+    const int e = sh.list[li][q];
+    const EventP<T>& E = sh.ev[e];
+    const Frame<T> f{E.fct, E.fst, E.fcp, E.fsp};
+    const T t2 = (upper ? E.a_up : E.a_dn) * g;
+    const T wgt = t2 <= tau0l ? MT<T>::exp2n(t2) * w : T(0);
+    T c[4][5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      T n1, m1, n2, m2;
+      fourier_node<T>(j, n1, m1, n2, m2);
+      T o[4];
+      rayleigh_peel<T>(st, ct, n1, m1, f, E.I, o);
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        if (j == 0) {
+          c[s][0] = o[s];
+          c[s][1] = o[s];
+          c[s][2] = T(0);
+          c[s][3] = o[s];
+          c[s][4] = T(0);
+        } else {
+          c[s][0] += o[s];
+          c[s][1] += o[s] * n1;
+          c[s][2] += o[s] * m1;
+          c[s][3] += o[s] * n2;
+          c[s][4] += o[s] * m2;
+        }
+      }
+    }
+    // f(phi) = c0/5 + (2/5) (c1 cos phi + c2 sin phi + c3 cos 2phi + c4 sin 2phi)
+    const T w0 = wgt * T(0.2), w1 = wgt * T(0.4);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      acc[s][0] += w0 * c[s][0];
+#pragma unroll
+      for (int m = 1; m < 5; ++m) acc[s][m] += w1 * c[s][m];
+    }
+    T esc = w0 * c[0][0] * fs0 + w1 * (c[0][1] * fs1 + c[0][2] * fs2 + c[0][3] * fs3 + c[0][4] * fs4);
+    esc = warp_sum(esc);
+    if (lane == 0) atomicAdd(&escarr[e], esc);
+  }
+  if (ok) {
+    double* dst = in.Frt + 20 * (size_t)j1;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int m = 0; m < 5; ++m) atomicAdd(dst + 5 * s + m, (double)acc[s][m]);
+  }
+}
+
+// Irt of every bin from the Fourier coefficients (plain stores: the Fourier path writes
+// Irt nowhere else). Coefficients are read through L2, after the caller's fence.
+template <typename T>
+__device__ void fourier_expand(const DevInstance& in, const BinTables<T>& B, int tid, int nthreads) {
+  const int nt = B.ntheta, nb = B.ntheta * B.nphi;
+  for (int b = tid; b < nb; b += nthreads) {
+    const int j1 = b % nt, j2 = b / nt;
+    const double cp = (double)B.cp[j2], sp = (double)B.sp[j2];
+    const double c2 = cp * cp - sp * sp, s2 = 2.0 * sp * cp;
+    const double* f = in.Frt + 20 * (size_t)j1;
+    double* dst = in.Irt + 4 * (size_t)b;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      dst[s] = __ldcg(f + 5 * s) + __ldcg(f + 5 * s + 1) * cp + __ldcg(f + 5 * s + 2) * sp +
+               __ldcg(f + 5 * s + 3) * c2 + __ldcg(f + 5 * s + 4) * s2;
   }
 }
 
@@ -1287,6 +1442,7 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
   if (tid == 0) {
     sh.cur = next_instance(p, -1);
     sh.exhausted = 0;
+    sh.taken = 0;
     sh.item_next = 0;
     for (int i = 0; i < 8; ++i) (&sh.cnt[0][0])[i] = 0;
   }
@@ -1308,7 +1464,12 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
       if (want) {
         const int leader = __ffs(want) - 1;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(in.claim, (unsigned long long)__popc(want));
+        if (lane == leader) {
+          const int nw = __popc(want);
+          base = atomicAdd(in.claim, (unsigned long long)nw);
+          const long long left = in.n_photons - (long long)base;
+          if (left > 0) atomicAdd(&sh.taken, left < nw ? (int)left : nw);
+        }
         base = __shfl_sync(0xffffffffu, base, leader);
         if (want_b) {
           unsigned long long my = base + __popc(want & ((1u << lane) - 1u));
@@ -1360,10 +1521,30 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
         v = warp_sum(v);
         if (lane == 0 && v != 0.0) atomicAdd(in.acc + k, v);
       }
+      if (in.rt_fourier) {
+        // Publish this block's coefficient flushes, then count its photons as finished;
+        // the block whose count completes the launch's photons expands the coefficients.
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+          int last = 0;
+          if (sh.taken > 0) {
+            const unsigned long long old = atomicAdd(in.claim + 1, (unsigned long long)sh.taken);
+            last = (long long)(old + (unsigned long long)sh.taken) == in.n_photons;
+          }
+          sh.expand = last;
+        }
+        __syncthreads();
+        if (sh.expand) {
+          __threadfence();
+          fourier_expand<T>(in, B, tid, BS);
+        }
+      }
       __syncthreads();
       if (tid == 0) {
         sh.cur = next_instance(p, sh.cur);
         sh.exhausted = 0;
+        sh.taken = 0;
         for (int i = 0; i < 8; ++i) (&sh.cnt[0][0])[i] = 0;
       }
       __syncthreads();
@@ -1375,13 +1556,20 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
     {
       const int nu = sh.cnt[pc][0], nd = sh.cnt[pc][1], nc = sh.cnt[pc][2] + sh.cnt[pc][3];
       const int tcb = nc ? (B.nphib * ((B.nthetab + NBC - 1) / NBC) + 31) / 32 : 0;
-      const int tup = nu ? (B.nphi * ((B.up1 - B.up0 + NBR - 1) / NBR) + 31) / 32 : 0;
-      const int tdn = nd ? (B.nphi * ((B.lo1 - B.lo0 + NBR - 1) / NBR) + 31) / 32 : 0;
+      const bool fr = sh.inst.rt_fourier != 0;
+      const int tup = !nu ? 0
+                      : fr ? (B.up1 - B.up0 + 31) / 32
+                           : (B.nphi * ((B.up1 - B.up0 + NBR - 1) / NBR) + 31) / 32;
+      const int tdn = !nd ? 0
+                      : fr ? (B.lo1 - B.lo0 + 31) / 32
+                           : (B.nphi * ((B.lo1 - B.lo0 + NBR - 1) / NBR) + 31) / 32;
       // Work items are (tile, chunk of up to EVC events); the costlier CB items go first.
       // Chunks only split batches larger than 256 events: below that, the extra tally
-      // flushes cost more than the better balance gains.
-      constexpr int EVC = 256;
-      const int ccb = (nc + EVC - 1) / EVC, cup = (nu + EVC - 1) / EVC, cdn = (nd + EVC - 1) / EVC;
+      // flushes cost more than the better balance gains. Fourier RT tiles are few (one
+      // lane per polar bin) and flush 20 values per lane, so they take smaller chunks.
+      constexpr int EVC = 256, EVF = 64;
+      const int evr = fr ? EVF : EVC;
+      const int ccb = (nc + EVC - 1) / EVC, cup = (nu + evr - 1) / evr, cdn = (nd + evr - 1) / evr;
       const int icb = tcb * ccb, iup = tup * cup, idn = tdn * cdn;
       const int total = icb + iup + idn;
       if (tid == 0)
@@ -1400,14 +1588,18 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
         } else if (w < icb + iup) {
           w -= icb;
           const int c = w % cup;
-          if constexpr (std::is_same<T, float>::value)
+          if (fr)
+            rt_fourier_tile<T, BS>(sh, B, w / cup, true, c * evr, min((c + 1) * evr, nu));
+          else if constexpr (std::is_same<T, float>::value)
             rt_tile_f2<NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
           else
             rt_tile<T, NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
         } else {
           w -= icb + iup;
           const int c = w % cdn;
-          if constexpr (std::is_same<T, float>::value)
+          if (fr)
+            rt_fourier_tile<T, BS>(sh, B, w / cdn, false, c * evr, min((c + 1) * evr, nd));
+          else if constexpr (std::is_same<T, float>::value)
             rt_tile_f2<NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
           else
             rt_tile<T, NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));

@@ -32,7 +32,7 @@ def small_cfg(M, g, n, **kw):
 
 def geometry(M, case, mie5, mie2):
     ray = M.RayleighScatterer(0.99, 100.0)
-    if case == "plane_rayleigh":
+    if case in ("plane_rayleigh", "plane_rayleigh_nphi4", "plane_rayleigh_full_bins"):
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), N0
     if case == "plane_rayleigh_V":
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), [1, 0, 0, -1]
@@ -49,13 +49,18 @@ def geometry(M, case, mie5, mie2):
     raise ValueError(case)
 
 
-CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite"]
+CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite",
+         "plane_rayleigh_nphi4", "plane_rayleigh_full_bins"]
+# Bin grids other than small_cfg's. A slab of Rayleigh scatterers tallies RT through
+# azimuthal Fourier modes when Nphi >= 5; Nphi = 4 keeps the per-bin evaluation, and the
+# full grid is the reference's default (64 x 48 RT bins).
+CASE_BINS = {"plane_rayleigh_nphi4": {"Nphi": 4}, "plane_rayleigh_full_bins": {"Ntheta": 64, "Nphi": 48}}
 
 
 @pytest.mark.parametrize("case", CASES)
 def test_fp64_kernels_match_oracle_on_same_streams(M, O, gpu_ctx, mie5, mie2, case):
     g, I0 = geometry(M, case, mie5, mie2)
-    cfg = small_cfg(M, g, 600)
+    cfg = small_cfg(M, g, 600, **CASE_BINS.get(case, {}))
     n = cfg.number_of_rays
     ref = O.simulate(cfg, g, I0, seed=21, threads=0)
     for kernel in ("persistent", "plain"):
@@ -74,10 +79,10 @@ def test_fp64_kernels_match_oracle_on_same_streams(M, O, gpu_ctx, mie5, mie2, ca
         assert abs(A.sum() - 1) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["plane_rayleigh", "plane_mie_oblique", "sphere_mie"])
+@pytest.mark.parametrize("case", ["plane_rayleigh", "plane_mie_oblique", "sphere_mie", "plane_rayleigh_full_bins"])
 def test_fp32_matches_fp64_on_same_streams(M, gpu_ctx, mie5, mie2, case):
     g, I0 = geometry(M, case, mie5, mie2)
-    cfg = small_cfg(M, g, 1 << 14)
+    cfg = small_cfg(M, g, 1 << 14, **CASE_BINS.get(case, {}))
     o64 = M.simulate(cfg, g, I0, precision="fp64", seed=5, with_extras=True)
     o32 = M.simulate(cfg, g, I0, precision="fp32", seed=5, with_extras=True)
     A64, R64, C64 = sim_arrays(o64)

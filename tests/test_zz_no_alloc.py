@@ -35,13 +35,17 @@ def _call(M, name, ctx, cfg, g, I0, opts):
     return A, Irt, Icb, lad, st.as_dict()
 
 
+@pytest.mark.parametrize("scat", ["mie", "rayleigh"])
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
-def test_noalloc_entry_point_matches_simulate_twice(M, prec, tol):
+def test_noalloc_entry_point_matches_simulate_twice(M, prec, tol, scat):
     if M.lib().mcrt_device_count() <= 0:
         pytest.fail("needs a CUDA device")
     ctx = M.Context(0)
-    mie = M.MieScatterer(5.0 / (2 * math.pi), 1.5 + 0.001j, 1.0, 0.1, Ntheta=1801)
-    g = M.PlaneGeometry(math.radians(150.0), 0.0, [M.Layer(d=3.0 * mie.kl, scatterer=mie)])
+    if scat == "mie":
+        sc = M.MieScatterer(5.0 / (2 * math.pi), 1.5 + 0.001j, 1.0, 0.1, Ntheta=1801)
+    else:  # a Rayleigh slab tallies RT through azimuthal Fourier modes
+        sc = M.RayleighScatterer(0.99, 100.0)
+    g = M.PlaneGeometry(math.radians(150.0), 0.0, [M.Layer(d=3.0 * sc.kl, scatterer=sc)])
     cfg = M.Config(g, number_of_rays=3000, Ntheta=16, Nphi=8, Nphib=4,
                    thetab=np.deg2rad(np.linspace(0, 3, 12)), maximum_scattering_times=500)
     I0 = [1.0, 0.0, 0.0, 1.0]
