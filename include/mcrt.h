@@ -215,6 +215,24 @@ int mcrt_batch_read(mcrt_batch* b, int i, double A_out[5], double* Irt, double* 
 int mcrt_batch_timing(mcrt_batch* b, double* kernel_ms, double* photons);
 int mcrt_batch_destroy(mcrt_batch* b);
 
+/* ------------------------------------------------------------------ run_rt */
+/* run_rt(cfg, g) of src/MonteCarloRadiativeTransfer.jl:87-291: the Mueller matrices of
+ * the reflected (RT) and coherently backscattered (CB) light. The reference calls
+ * simulate once per incident polarisation state (plane.jl:70-75: 6 states; sphere.jl:
+ * 49-52: 2 states); here the states run as one batched launch (state i with Philox
+ * instance opts->instance + i, the same stream as an mcrt_simulate with that instance)
+ * and a device epilogue assembles the matrices from the device tallies.
+ * Outputs (caller-allocated host memory), element s_ab at index 4(a-1)+(b-1):
+ *   plane:  M_rt[16][Nphi][Ntheta], M_cb[16][Nphi_b][Ntheta_b] (the reference's
+ *           DataFrame rows, theta fastest);
+ *   sphere: M_rt[16][Ntheta], M_cb[16][Ntheta_b].
+ *   energy[5] = {direct transmission, absorption, reflection, transmission (0 for a
+ *   sphere), remaining}: the G sums that the reference logs (MonteCarloRadiativeTransfer.jl
+ *   :113-118 and :161-165 for a sphere, :217-223 and :250-255 for a plane).
+ * stats (optional) sums the states' counters. Persistent kernel only. */
+int mcrt_run_rt(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g, const mcrt_run_opts* opts,
+                double* M_rt, double* M_cb, double energy[5], mcrt_stats* stats);
+
 /* ------------------------------------------------------------------ serving loop */
 /* A continuous-batching request loop in front of the persistent kernel. Requests (each
  * a simulate() instance with its own config, geometry, scatterers, I0, seed and photon

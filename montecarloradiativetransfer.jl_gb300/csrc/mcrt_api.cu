@@ -997,6 +997,219 @@ int mcrt_batch_destroy(mcrt_batch* b) {
 
 }  // extern "C"
 
+// ================================================================== run_rt
+namespace {
+
+// Inputs of the Mueller assembly epilogue. The tallies of state i start at
+// tally + i * per_inst (Irt | Icb | ladder | acc, raw sums).
+struct RunRtArgs {
+  int kind;
+  int n_states;
+  int nt, np, ntb, npb;
+  size_t per_inst, nrt, ncb;
+  const double* tally;
+  double inv_n;            // 1 / number_of_rays
+  const double* norm_rt;   // per theta: plane |1/(4 cos inorm)|, sphere 1/inorm
+  const double* norm_cb;   // per theta_b: plane 1/|4 cos|, sphere 1
+  double* out_rt;          // plane [16][np][nt], sphere [16][nt]
+  double* out_cb;          // plane [16][npb][ntb], sphere [16][ntb]
+  double coef[6][4];       // plane: weight of state i's tally in Mueller column b
+  int vstate[2];           // sphere: state i has V != 0
+  int nfi[8], nfib[8];     // sphere: the 8 azimuth indices i * Nphi / 8
+};
+
+// Plane assembly of MonteCarloRadiativeTransfer.jl:186-291: one thread per RT or CB bin.
+__global__ void k_run_rt_plane(RunRtArgs a) {
+  const int nrt = a.nt * a.np, ncb = a.ntb * a.npb;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrt + ncb) return;
+  const bool rt = t < nrt;
+  const int b = rt ? t : t - nrt;  // bin index j2 * ntheta + j1
+  const size_t off = rt ? 0 : a.nrt;
+  const double nrm = (rt ? a.norm_rt[b % a.nt] : a.norm_cb[b % a.ntb]) * a.inv_n;
+  double m[4][4] = {};
+  for (int i = 0; i < a.n_states; ++i) {
+    const double* x = a.tally + (size_t)i * a.per_inst + off + 4 * (size_t)b;
+    for (int s = 0; s < 4; ++s)
+      for (int c = 0; c < 4; ++c) m[s][c] += a.coef[i][c] * x[s];
+  }
+  double* out = rt ? a.out_rt : a.out_cb;
+  const int nb = rt ? nrt : ncb;
+  for (int s = 0; s < 4; ++s)
+    for (int c = 0; c < 4; ++c) out[(size_t)(4 * s + c) * nb + b] = m[s][c] * nrm;
+}
+
+// Sphere assembly of MonteCarloRadiativeTransfer.jl:87-184: one thread per RT or CB
+// polar bin, summing over azimuths; renormalised by the scattered energy.
+__global__ void k_run_rt_sphere(RunRtArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.nt + a.ntb) return;
+  const bool rt = t < a.nt;
+  const int j1 = rt ? t : t - a.nt;
+  const int nt = rt ? a.nt : a.ntb, np = rt ? a.np : a.npb;
+  const int* N = rt ? a.nfi : a.nfib;
+  const size_t off = rt ? 0 : a.nrt;
+  double gsca = 0.0;
+  for (int i = 0; i < a.n_states; ++i)
+    if (!a.vstate[i]) {
+      const double* acc = a.tally + (size_t)i * a.per_inst + a.nrt + a.ncb + a.ncb / 4;
+      gsca += (acc[ACC_ADT] + acc[ACC_AREF]) * a.inv_n;
+    }
+  double m[4][4] = {};
+  for (int i = 0; i < a.n_states; ++i) {
+    const double* x = a.tally + (size_t)i * a.per_inst + off;
+    auto X = [&](int s, int p) { return x[4 * ((size_t)p * nt + j1) + s] * a.inv_n; };
+    if (!a.vstate[i]) {
+      for (int s = 0; s < 4; ++s) {
+        m[s][0] += (X(s, N[0]) + X(s, N[2]) + X(s, N[4]) + X(s, N[6])) * 0.25;
+        m[s][1] += (-X(s, N[0]) + X(s, N[2]) - X(s, N[4]) + X(s, N[6])) * 0.25;
+        m[s][2] += (X(s, N[1]) - X(s, N[3]) + X(s, N[5]) - X(s, N[7])) * 0.25;
+      }
+    } else {
+      m[2][3] -= (X(2, N[0]) + X(2, N[4])) * 0.5;
+      double s3 = 0.0;
+      for (int p = 0; p < np; ++p) s3 += X(3, p);
+      m[3][3] -= s3 / np;
+    }
+  }
+  const double nrm = (rt ? a.norm_rt[j1] : a.norm_cb[j1]) / gsca;
+  double* out = rt ? a.out_rt : a.out_cb;
+  for (int s = 0; s < 4; ++s)
+    for (int c = 0; c < 4; ++c) out[(size_t)(4 * s + c) * nt + j1] = m[s][c] * nrm;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcrt_run_rt(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g, const mcrt_run_opts* opts,
+                double* M_rt, double* M_cb, double energy[5], mcrt_stats* stats) {
+  if (!ctx || !cfg || !g || !M_rt || !M_cb || !energy)
+    return set_err(MCRT_EINVAL, "mcrt_run_rt: NULL argument");
+  if (opts && opts->kernel == MCRT_KERNEL_PLAIN)
+    return set_err(MCRT_EINVAL, "mcrt_run_rt runs the persistent kernel (one batched launch)");
+  int rc = validate_geometry(g);
+  if (rc) return rc;
+  rc = validate_config(cfg, g->kind);
+  if (rc) return rc;
+  // incident states: plane.jl:70-75 (6, columns) and sphere.jl:49-52 (2)
+  static const double IP[6][4] = {{1, -1, 0, 0}, {1, 1, 0, 0}, {1, 0, -1, 0},
+                                  {1, 0, 1, 0},  {1, 0, 0, -1}, {1, 0, 0, 1}};
+  static const double IS[2][4] = {{1, -1, 0, 0}, {1, 0, 0, -1}};
+  const bool plane = g->kind == MCRT_PLANE;
+  const int n = plane ? 6 : 2;
+  std::vector<const mcrt_geometry*> gs(n, g);
+  std::vector<double> I(4 * (size_t)n);
+  std::vector<uint64_t> seeds(n, opts ? opts->seed : 0);
+  std::vector<uint32_t> ids(n);
+  std::vector<long long> nph(n, cfg->number_of_rays);
+  for (int i = 0; i < n; ++i) {
+    for (int s = 0; s < 4; ++s) I[4 * i + s] = plane ? IP[i][s] : IS[i][s];
+    ids[i] = (opts ? opts->instance : 0) + (uint32_t)i;
+  }
+  CK(cudaSetDevice(ctx->device));
+  Group G;
+  rc = build_group(ctx, cfg, gs.data(), reinterpret_cast<const double(*)[4]>(I.data()), seeds.data(), ids.data(),
+                   nph.data(), opts ? opts->photon_begin : 0, opts ? opts->rng_mode : 0, n, opts, G);
+  if (rc) return rc;
+  rc = launch_group(G);
+  if (rc) return rc;
+
+  RunRtArgs a{};
+  a.kind = g->kind;
+  a.n_states = n;
+  a.nt = cfg->n_theta;
+  a.np = cfg->n_phi;
+  a.ntb = cfg->n_theta_b;
+  a.npb = cfg->n_phi_b;
+  a.per_inst = G.per_inst;
+  a.nrt = G.nrt;
+  a.ncb = G.ncb;
+  a.tally = G.d_tally.as<double>();
+  a.inv_n = cfg->number_of_rays > 0 ? 1.0 / (double)cfg->number_of_rays : 0.0;
+  std::vector<double> nrm(a.nt + a.ntb);
+  for (int j = 0; j < a.nt; ++j)
+    nrm[j] = plane ? std::fabs(1.0 / (4.0 * cfg->cos_theta[j] * cfg->inorm[j])) : 1.0 / cfg->inorm[j];
+  for (int j = 0; j < a.ntb; ++j) nrm[a.nt + j] = plane ? 1.0 / std::fabs(4.0 * cfg->cos_theta_b[j]) : 1.0;
+  // first polarisation of each plane state (MonteCarloRadiativeTransfer.jl:208-215)
+  int k1s[6] = {0};
+  double k2s[6] = {0};
+  for (int i = 0; plane && i < n; ++i) {
+    for (int j = 1; j < 4; ++j)
+      if (std::fabs(I[4 * i + j]) > 1.0 - 2.220446049250313e-16) {
+        k1s[i] = j;
+        k2s[i] = I[4 * i + j];
+        break;
+      }
+    if (k1s[i] == 1) a.coef[i][0] += 0.5;
+    a.coef[i][k1s[i]] += 0.5 * k2s[i];
+  }
+  for (int i = 0; !plane && i < n; ++i) a.vstate[i] = I[4 * i + 3] != 0.0;
+  for (int i = 0; i < 8; ++i) {
+    a.nfi[i] = i * a.np / 8;
+    a.nfib[i] = i * a.npb / 8;
+  }
+  const size_t n_rt = 16 * (size_t)a.nt * (plane ? a.np : 1), n_cb = 16 * (size_t)a.ntb * (plane ? a.npb : 1);
+  DevBuf d_out;
+  CK(d_out.alloc((nrm.size() + n_rt + n_cb) * sizeof(double)));
+  double* dn = d_out.as<double>();
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(dn, nrm.data(), nrm.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  a.norm_rt = dn;
+  a.norm_cb = dn + a.nt;
+  a.out_rt = dn + nrm.size();
+  a.out_cb = a.out_rt + n_rt;
+  const int items = plane ? a.nt * a.np + a.ntb * a.npb : a.nt + a.ntb;
+  if (plane)
+    k_run_rt_plane<<<(items + 127) / 128, 128, 0, st>>>(a);
+  else
+    k_run_rt_sphere<<<(items + 127) / 128, 128, 0, st>>>(a);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(M_rt, a.out_rt, n_rt * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(M_cb, a.out_cb, n_cb * sizeof(double), cudaMemcpyDeviceToHost, st));
+  rc = finish_group(G);
+  if (rc) return rc;
+  // energies from the per-state A tallies
+  double e[5] = {0, 0, 0, 0, 0};
+  unsigned flags = 0;
+  mcrt_stats tot;
+  std::memset(&tot, 0, sizeof tot);
+  for (int i = 0; i < n; ++i) {
+    double A[5];
+    mcrt_stats si;
+    rc = read_instance(G, i, A, nullptr, nullptr, nullptr, &si);
+    if (rc) return rc;
+    flags |= (unsigned)si.status_flags;
+    tot.photons += si.photons;
+    tot.events += si.events;
+    tot.attempts += si.attempts;
+    tot.rt_evals += si.rt_evals;
+    tot.cb1_evals += si.cb1_evals;
+    tot.cbn_evals += si.cbn_evals;
+    tot.cb_peak_sum += si.cb_peak_sum;
+    tot.cb_peak_sumsq += si.cb_peak_sumsq;
+    tot.block_size = si.block_size;
+    tot.blocks = si.blocks;
+    tot.kernel_ms = si.kernel_ms;
+    if (plane && k1s[i] == 1)
+      for (int s = 0; s < 5; ++s) e[s] += 0.5 * A[s] * a.inv_n;
+    if (!plane && !a.vstate[i]) {
+      e[0] += A[0] * a.inv_n;
+      e[1] += A[1] * a.inv_n;
+      e[2] += A[2] * a.inv_n;
+      e[4] += A[4] * a.inv_n;
+    }
+  }
+  for (int s = 0; s < 5; ++s) energy[s] = e[s];
+  tot.status_flags = (int)flags;
+  if (stats) *stats = tot;
+  if (flags & MCRT_FLAG_REJECT_LIMIT)
+    return set_err(MCRT_ENONCONV, "a rejection loop hit its iteration cap; see stats.status_flags");
+  return MCRT_OK;
+}
+
+}  // extern "C"
+
 // ================================================================== FP32 peak
 namespace {
 // Eight independent FMA chains per thread; the result is stored only if it is

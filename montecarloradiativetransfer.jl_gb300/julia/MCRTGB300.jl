@@ -3,7 +3,8 @@
 
 Julia binding of libmcrt for MonteCarloRadiativeTransfer.jl: `MCRTGB300.simulate(cfg, g, I₀)`
 returns what the package's `simulate(cfg, g, I₀; use_gpu=true)` returns
-(src/MonteCarloRadiativeTransfer.jl:26-85), computed by libmcrt's CUDA kernels.
+(src/MonteCarloRadiativeTransfer.jl:26-85), and `MCRTGB300.run_rt(cfg, g)` what its
+`run_rt(cfg, g; use_gpu=true)` returns (:87-291), computed by libmcrt's CUDA kernels.
 
 The library path defaults to the in-tree build and can be overridden with the
 environment variable `MCRT_GB300_LIB`.
@@ -137,6 +138,25 @@ geometry_kind(::MCRT.SphereGeometry) = 1
 incidence(g::MCRT.PlaneGeometry) = (g.θ, g.ϕ)
 incidence(::MCRT.SphereGeometry) = (Float64(π), 0.0)
 
+# Marshals cfg and g into the C structs and calls f(c, gc) while the arrays are alive.
+function with_c(f, cfg::MCRT.Config, g)
+    arrays = map(a -> collect(Float64, a),
+                 (cfg.cosϕ, cfg.sinϕ, cfg.cosθ, cfg.sinθ, cfg.inorm, cfg.cosθb, cfg.sinθb,
+                  cfg.cosϕb, cfg.sinϕb))
+    Ls = layers_c(g)
+    θ, ϕ = incidence(g)
+    GC.@preserve arrays Ls begin
+        c = ConfigC(cfg.number_of_rays, cfg.minimum_intensity, cfg.maximum_scattering_times,
+                    cfg.maximum_threads, Cint(cfg.compute_cb), cfg.τ₀,
+                    cfg.Nϕ, pointer(arrays[1]), pointer(arrays[2]),
+                    cfg.Nθ, pointer(arrays[3]), pointer(arrays[4]), pointer(arrays[5]),
+                    cfg.Nθb, pointer(arrays[6]), pointer(arrays[7]),
+                    cfg.Nϕb, pointer(arrays[8]), pointer(arrays[9]))
+        gc = GeometryC(geometry_kind(g), θ, ϕ, length(Ls), pointer(Ls))
+        return f(c, gc)
+    end
+end
+
 """
     simulate(cfg, g, I₀; precision = 0, seed = rand(UInt64), instance = 0)
 
@@ -145,30 +165,54 @@ The GPU branch of `simulate` (src/MonteCarloRadiativeTransfer.jl:36-56): returns
 `Irt::Array{Float64,3}` of size (4, Nθ, Nϕ) and `Icb` of size (4, Nθb, Nϕb).
 """
 function simulate(cfg::MCRT.Config, g, I₀; precision = 0, seed = rand(UInt64), instance = 0)
-    arrays = map(a -> collect(Float64, a),
-                 (cfg.cosϕ, cfg.sinϕ, cfg.cosθ, cfg.sinθ, cfg.inorm, cfg.cosθb, cfg.sinθb,
-                  cfg.cosϕb, cfg.sinϕb))
-    Ls = layers_c(g)
-    θ, ϕ = incidence(g)
     I = collect(Float64, I₀)
     A = zeros(5)
     Irt = zeros(4, cfg.Nθ, cfg.Nϕ)
     Icb = zeros(4, cfg.Nθb, cfg.Nϕb)
     opts = RunOpts(; precision, seed, instance)
-    GC.@preserve arrays Ls I A Irt Icb begin
-        c = ConfigC(cfg.number_of_rays, cfg.minimum_intensity, cfg.maximum_scattering_times,
-                    cfg.maximum_threads, Cint(cfg.compute_cb), cfg.τ₀,
-                    cfg.Nϕ, pointer(arrays[1]), pointer(arrays[2]),
-                    cfg.Nθ, pointer(arrays[3]), pointer(arrays[4]), pointer(arrays[5]),
-                    cfg.Nθb, pointer(arrays[6]), pointer(arrays[7]),
-                    cfg.Nϕb, pointer(arrays[8]), pointer(arrays[9]))
-        gc = GeometryC(geometry_kind(g), θ, ϕ, length(Ls), pointer(Ls))
+    with_c(cfg, g) do c, gc
         check(ccall((:mcrt_simulate, libmcrt), Cint,
                     (Ptr{Cvoid}, Ref{ConfigC}, Ref{GeometryC}, Ptr{Float64}, Ref{RunOpts},
                      Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Cvoid}),
                     context(), c, gc, I, opts, A, Irt, Icb, C_NULL, C_NULL))
     end
     return A[1], A[2], A[3], A[4], A[5], Irt, Icb
+end
+
+"""
+    run_rt(cfg, g; precision = 0, seed = rand(UInt64))
+
+`run_rt(cfg, g; use_gpu = true)` (src/MonteCarloRadiativeTransfer.jl:87-291): the RT and
+CB Mueller-matrix DataFrames, with all incident polarisation states in one batched
+launch and the matrices assembled on the device (`mcrt_run_rt`).
+"""
+function run_rt(cfg::MCRT.Config, g; precision = 0, seed = rand(UInt64))
+    plane = g isa MCRT.PlaneGeometry
+    nrt = cfg.Nθ * (plane ? cfg.Nϕ : 1)
+    ncb = cfg.Nθb * (plane ? cfg.Nϕb : 1)
+    Mrt = zeros(nrt, 16)            # C layout [16][rows] is Julia's (rows, 16)
+    Mcb = zeros(ncb, 16)
+    E = zeros(5)
+    opts = RunOpts(; precision, seed, instance = 0)
+    with_c(cfg, g) do c, gc
+        check(ccall((:mcrt_run_rt, libmcrt), Cint,
+                    (Ptr{Cvoid}, Ref{ConfigC}, Ref{GeometryC}, Ref{RunOpts}, Ptr{Float64},
+                     Ptr{Float64}, Ptr{Float64}, Ptr{Cvoid}),
+                    context(), c, gc, opts, Mrt, Mcb, E, C_NULL))
+    end
+    cols(M) = [Symbol(:s, i, j) => M[:, 4 * (i - 1) + j] for i in 1:4 for j in 1:4]
+    θ = 180.0 / π * acos.(collect(cfg.cosθ))
+    θb = 180.0 / π * acos.(collect(cfg.cosθb))
+    if plane
+        SM_rt = MCRT.DataFrame(:θ => repeat(θ; outer = cfg.Nϕ),
+                               :ϕ => repeat(180.0 / π * collect(cfg.ϕ); inner = cfg.Nθ), cols(Mrt)...)
+        SM_cb = MCRT.DataFrame(:θ => repeat(θb; outer = cfg.Nϕb),
+                               :ϕ => repeat(180.0 / π * collect(cfg.ϕb); inner = cfg.Nθb), cols(Mcb)...)
+    else
+        SM_rt = MCRT.DataFrame(:θ => θ, cols(Mrt)...)
+        SM_cb = MCRT.DataFrame(:θ => θb, cols(Mcb)...)
+    end
+    return SM_rt, SM_cb
 end
 
 end # module

@@ -330,90 +330,57 @@ class Server:
 
 
 # ------------------------------------------------------------------ run_rt
-def _first_polarisation(I) -> Tuple[int, float]:
-    for j1 in range(1, 4):  # MonteCarloRadiativeTransfer.jl:208-215
-        if abs(I[j1]) > 1.0 - np.finfo(float).eps:
-            return j1, float(I[j1])
-    return 0, 0.0
-
-
-def run_rt(cfg, g, *, use_gpu: bool = True, ctx: Optional[Context] = None, **opts):
+def run_rt(cfg, g, *, use_gpu: bool = True, ctx: Optional[Context] = None, with_stats: bool = False, **opts):
     """run_rt (src/MonteCarloRadiativeTransfer.jl:87-291): the Mueller matrices of the
     reflected (RT) and coherently backscattered (CB) light, as dicts of columns
     ``theta`` (and ``phi`` for a plane), ``s11`` ... ``s44``, plus an ``energy`` dict.
 
-    Each incident polarisation state is one simulate() call with its own Philox key
-    word (``instance`` = state index)."""
+    All incident polarisation states run in one batched launch of the persistent kernel
+    (state i with Philox ``instance + i``) and a device epilogue assembles the matrices
+    (mcrt_run_rt). With ``with_stats`` a fourth element holds the summed launch stats."""
+    if not use_gpu:
+        raise NotImplementedError(
+            "this package runs the transport on the GPU only; the CPU path is the reference's")
+    ctx = ctx or default_context()
     g.validate()
-    IS = g.initial_I()
-    seed = opts.pop("seed", 1)
-    if g.kind == _lib.SPHERE:
-        return _run_rt_sphere(cfg, g, IS, seed, use_gpu, ctx, opts)
-    return _run_rt_plane(cfg, g, IS, seed, use_gpu, ctx, opts)
-
-
-def _run_rt_sphere(cfg, g, IS, seed, use_gpu, ctx, opts):
-    Nphi, Nphib = cfg.Nphi, cfg.Nphib
-    NFI = [i * Nphi // 8 for i in range(8)]
-    NFIB = [i * Nphib // 8 for i in range(8)]
-    G = np.zeros(4)  # dt, abs, ref, rem
-    MRT = np.zeros((4, 4, cfg.Ntheta))
-    MCB = np.zeros((4, 4, cfg.Nthetab))
-    for i in range(IS.shape[1]):
-        I = IS[:, i]
-        Adt, Aabs, Aref, _, Arem, IRT, ICB = simulate(cfg, g, I, use_gpu=use_gpu, ctx=ctx, seed=seed,
-                                                      instance=i, **opts)
-        if I[3] == 0:
-            G += [Adt, Aabs, Aref, Arem]
-            for M, X, N in ((MRT, IRT, NFI), (MCB, ICB, NFIB)):
-                M[:, 0, :] += (X[:, :, N[0]] + X[:, :, N[2]] + X[:, :, N[4]] + X[:, :, N[6]]) * 0.25
-                M[:, 1, :] += (-X[:, :, N[0]] + X[:, :, N[2]] - X[:, :, N[4]] + X[:, :, N[6]]) * 0.25
-                M[:, 2, :] += (X[:, :, N[1]] - X[:, :, N[3]] + X[:, :, N[5]] - X[:, :, N[7]]) * 0.25
-        else:
-            for M, X, N, n in ((MRT, IRT, NFI, Nphi), (MCB, ICB, NFIB, Nphib)):
-                M[2, 3, :] -= (X[2, :, N[0]] + X[2, :, N[4]]) * 0.5
-                M[3, 3, :] -= X[3, :, :].sum(axis=1) / n
-    Gsca = G[0] + G[2]
-    renorm = 1.0 / Gsca
-    MRT *= renorm * (1.0 / cfg.inorm)[None, None, :]
-    MCB *= renorm
-    sm_rt = {"theta": 180.0 / math.pi * np.arccos(cfg.costheta)}
-    sm_cb = {"theta": 180.0 / math.pi * np.arccos(cfg.costhetab)}
-    for a in range(4):
-        for b in range(4):
-            sm_rt[f"s{a + 1}{b + 1}"] = MRT[a, b, :].copy()
-            sm_cb[f"s{a + 1}{b + 1}"] = MCB[a, b, :].copy()
-    energy = {"direct_transmission": G[0], "absorption": G[1], "reflection": G[2], "remaining": G[3]}
-    return sm_rt, sm_cb, energy
-
-
-def _run_rt_plane(cfg, g, IS, seed, use_gpu, ctx, opts):
-    G = np.zeros(5)
-    MRT = np.zeros((4, 4, cfg.Ntheta, cfg.Nphi))
-    MCB = np.zeros((4, 4, cfg.Nthetab, cfg.Nphib))
-    for i in range(IS.shape[1]):
-        I = IS[:, i]
-        Adt, Aabs, Aref, Atrans, Arem, IRT, ICB = simulate(cfg, g, I, use_gpu=use_gpu, ctx=ctx, seed=seed,
-                                                           instance=i, **opts)
-        k1, k2 = _first_polarisation(I)
-        if k1 == 1:
-            G += np.array([Adt, Aabs, Aref, Atrans, Arem]) / 2.0
-            MRT[:, 0] += IRT / 2.0
-            MCB[:, 0] += ICB / 2.0
-        MRT[:, k1] += k2 * IRT / 2.0
-        MCB[:, k1] += k2 * ICB / 2.0
-    norm = np.abs(1.0 / (4.0 * cfg.costheta * cfg.inorm))  # MonteCarloRadiativeTransfer.jl:259
-    MRT *= norm[None, None, :, None]
-    norm1 = 1.0 / np.abs(4.0 * cfg.costhetab)  # :273-278
-    MCB *= norm1[None, None, :, None]
+    cc = cfg.to_c()
+    gc, keep = ctx.geometry_c(g)
+    plane = g.kind != _lib.SPHERE
+    nrt = 16 * cfg.Ntheta * (cfg.Nphi if plane else 1)
+    ncb = 16 * cfg.Nthetab * (cfg.Nphib if plane else 1)
+    Mrt, Mcb, E = np.zeros(nrt), np.zeros(ncb), np.zeros(5)
+    st = _lib.Stats()
+    o = run_opts(**opts)
+    check(lib().mcrt_run_rt(ctx.h, C.byref(cc), C.byref(gc), C.byref(o), dptr(Mrt), dptr(Mcb), dptr(E),
+                            C.byref(st)))
+    Mrt = Mrt.reshape(16, -1)
+    Mcb = Mcb.reshape(16, -1)
     th = 180.0 / math.pi * np.arccos(cfg.costheta)
     thb = 180.0 / math.pi * np.arccos(cfg.costhetab)
-    sm_rt = {"theta": np.tile(th, cfg.Nphi), "phi": np.repeat(180.0 / math.pi * cfg.phi, cfg.Ntheta)}
-    sm_cb = {"theta": np.tile(thb, cfg.Nphib), "phi": np.repeat(180.0 / math.pi * cfg.phib, cfg.Nthetab)}
+    if plane:
+        sm_rt = {"theta": np.tile(th, cfg.Nphi), "phi": np.repeat(180.0 / math.pi * cfg.phi, cfg.Ntheta)}
+        sm_cb = {"theta": np.tile(thb, cfg.Nphib), "phi": np.repeat(180.0 / math.pi * cfg.phib, cfg.Nthetab)}
+        energy = {"direct_transmission": E[0], "absorption": E[1], "reflection": E[2], "transmission": E[3],
+                  "remaining": E[4]}
+    else:
+        sm_rt, sm_cb = {"theta": th}, {"theta": thb}
+        energy = {"direct_transmission": E[0], "absorption": E[1], "reflection": E[2], "remaining": E[4]}
     for a in range(4):
         for b in range(4):
-            sm_rt[f"s{a + 1}{b + 1}"] = MRT[a, b].reshape(-1, order="F").copy()
-            sm_cb[f"s{a + 1}{b + 1}"] = MCB[a, b].reshape(-1, order="F").copy()
-    energy = {"direct_transmission": G[0], "absorption": G[1], "reflection": G[2], "transmission": G[3],
-              "remaining": G[4]}
+            sm_rt[f"s{a + 1}{b + 1}"] = Mrt[4 * a + b].copy()
+            sm_cb[f"s{a + 1}{b + 1}"] = Mcb[4 * a + b].copy()
+    if with_stats:
+        return sm_rt, sm_cb, energy, st.as_dict()
     return sm_rt, sm_cb, energy
+
+
+def write_csv(table: dict, path: str) -> None:
+    """Writes a run_rt table (the reference's DataFrame columns ``θ, ϕ, s11 .. s44``,
+    src/MonteCarloRadiativeTransfer.jl:176-182, 280-290) as CSV with those headers."""
+    cols = [k for k in ("theta", "phi") if k in table] + [f"s{a}{b}" for a in range(1, 5) for b in range(1, 5)]
+    names = {"theta": "θ", "phi": "ϕ"}
+    data = np.column_stack([np.asarray(table[c], float) for c in cols])
+    with open(path, "w", encoding="utf-8") as f:
+        f.write(",".join(names.get(c, c) for c in cols) + "\n")
+        for row in data:
+            f.write(",".join(repr(float(v)) for v in row) + "\n")

@@ -31,3 +31,66 @@ def cb_peak_stats(stats):
     mu = stats["cb_peak_sum"] / n
     var = max(stats["cb_peak_sumsq"] / n - mu * mu, 0.0)
     return mu, math.sqrt(var)
+
+
+# ------------------------------------------------------------------ run_rt restatement
+# The checker for mcrt_run_rt: the Mueller assembly of src/MonteCarloRadiativeTransfer.jl
+# :87-291 in numpy, fed by one simulate-like call per incident state. ``sim(I, i)``
+# returns (Adt, Aabs, Aref, Atrans, Arem, Irt (4, Ntheta, Nphi), Icb (4, Ntheta_b, Nphi_b))
+# already divided by number_of_rays.
+def first_polarisation(I):
+    for j1 in range(1, 4):  # MonteCarloRadiativeTransfer.jl:208-215
+        if abs(I[j1]) > 1.0 - np.finfo(float).eps:
+            return j1, float(I[j1])
+    return 0, 0.0
+
+
+def assemble_run_rt(cfg, g, sim):
+    """(Mrt, Mcb, energy[5]) with Mrt of shape (4, 4, Ntheta, Nphi) for a plane and
+    (4, 4, Ntheta) for a sphere (Mcb likewise), energy = (dt, abs, ref, trans, rem)."""
+    IS = g.initial_I()
+    if g.kind == 1:  # sphere, :87-184
+        NFI = [i * cfg.Nphi // 8 for i in range(8)]
+        NFIB = [i * cfg.Nphib // 8 for i in range(8)]
+        G = np.zeros(5)
+        MRT = np.zeros((4, 4, cfg.Ntheta))
+        MCB = np.zeros((4, 4, cfg.Nthetab))
+        for i in range(IS.shape[1]):
+            I = IS[:, i]
+            Adt, Aabs, Aref, _, Arem, IRT, ICB = sim(I, i)
+            if I[3] == 0:
+                G += [Adt, Aabs, Aref, 0.0, Arem]
+                for M, X, N in ((MRT, IRT, NFI), (MCB, ICB, NFIB)):
+                    M[:, 0, :] += (X[:, :, N[0]] + X[:, :, N[2]] + X[:, :, N[4]] + X[:, :, N[6]]) * 0.25
+                    M[:, 1, :] += (-X[:, :, N[0]] + X[:, :, N[2]] - X[:, :, N[4]] + X[:, :, N[6]]) * 0.25
+                    M[:, 2, :] += (X[:, :, N[1]] - X[:, :, N[3]] + X[:, :, N[5]] - X[:, :, N[7]]) * 0.25
+            else:
+                for M, X, N, n in ((MRT, IRT, NFI, cfg.Nphi), (MCB, ICB, NFIB, cfg.Nphib)):
+                    M[2, 3, :] -= (X[2, :, N[0]] + X[2, :, N[4]]) * 0.5
+                    M[3, 3, :] -= X[3, :, :].sum(axis=1) / n
+        renorm = 1.0 / (G[0] + G[2])
+        MRT *= renorm * (1.0 / cfg.inorm)[None, None, :]
+        MCB *= renorm
+        return MRT, MCB, G
+    G = np.zeros(5)  # plane, :186-291
+    MRT = np.zeros((4, 4, cfg.Ntheta, cfg.Nphi))
+    MCB = np.zeros((4, 4, cfg.Nthetab, cfg.Nphib))
+    for i in range(IS.shape[1]):
+        I = IS[:, i]
+        Adt, Aabs, Aref, Atrans, Arem, IRT, ICB = sim(I, i)
+        k1, k2 = first_polarisation(I)
+        if k1 == 1:
+            G += np.array([Adt, Aabs, Aref, Atrans, Arem]) / 2.0
+            MRT[:, 0] += IRT / 2.0
+            MCB[:, 0] += ICB / 2.0
+        MRT[:, k1] += k2 * IRT / 2.0
+        MCB[:, k1] += k2 * ICB / 2.0
+    MRT *= np.abs(1.0 / (4.0 * cfg.costheta * cfg.inorm))[None, None, :, None]  # :259
+    MCB *= (1.0 / np.abs(4.0 * cfg.costhetab))[None, None, :, None]  # :273-278
+    return MRT, MCB, G
+
+
+def table_of(M, plane):
+    """The s_ab columns of an assembled matrix in run_rt's row order (theta fastest)."""
+    return {f"s{a + 1}{b + 1}": (M[a, b].reshape(-1, order="F") if plane else M[a, b])
+            for a in range(4) for b in range(4)}

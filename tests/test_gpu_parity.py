@@ -236,18 +236,43 @@ def test_full_size_workload_properties(M, gpu_ctx, mie5):
     assert scaled_err(tot, out[5]) < 1e-6
 
 
-def test_run_rt_on_gpu(M, gpu_ctx, mie2):
+@pytest.mark.parametrize("geom", ["plane_rayleigh", "plane_mie", "sphere_mie"])
+def test_run_rt_matches_per_state_simulate(M, gpu_ctx, mie5, mie2, geom):
+    """mcrt_run_rt (one batched launch + device Mueller assembly) against the numpy
+    restatement of run_rt fed by one FP64 simulate per incident state on the same
+    Philox streams."""
+    from helpers import assemble_run_rt, table_of
+
     ray = M.RayleighScatterer(0.99, 100.0)
-    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=2 * ray.kl, scatterer=ray)])
+    if geom == "plane_rayleigh":
+        g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=2 * ray.kl, scatterer=ray)])
+    elif geom == "plane_mie":
+        g = M.PlaneGeometry(math.radians(160), 0.3, [M.Layer(d=2 * mie5.kl, scatterer=mie5)])
+    else:
+        g = M.SphereGeometry(R=2 * mie2.kl, scatterer=mie2)
     cfg = small_cfg(M, g, 2000)
-    sm_rt, sm_cb, energy = M.run_rt(cfg, g)
-    assert len(sm_rt["s11"]) == cfg.Ntheta * cfg.Nphi
+    plane = g.kind == 0
+    sm_rt, sm_cb, energy, st = M.run_rt(cfg, g, seed=9, precision="fp64", with_stats=True)
+    assert st["status_flags"] & 5 == 0
+    assert st["photons"] == cfg.number_of_rays * (6 if plane else 2)
+
+    def sim(I, i):
+        return M.simulate(cfg, g, I, seed=9, instance=i, precision="fp64")
+
+    MRT, MCB, G = assemble_run_rt(cfg, g, sim)
+    ref_rt, ref_cb = table_of(MRT, plane), table_of(MCB, plane)
+    scale_rt = max(np.max(np.abs(v)) for v in ref_rt.values())
+    scale_cb = max(np.max(np.abs(v)) for v in ref_cb.values())
+    for k in ref_rt:
+        assert np.max(np.abs(sm_rt[k] - ref_rt[k])) <= 1e-9 * scale_rt, k
+        assert np.max(np.abs(sm_cb[k] - ref_cb[k])) <= 1e-9 * scale_cb, k
+    E = [energy["direct_transmission"], energy["absorption"], energy["reflection"],
+         energy.get("transmission", 0.0), energy["remaining"]]
+    assert np.allclose(E, G, rtol=1e-12, atol=1e-15)
     assert np.all(np.isfinite(sm_rt["s11"]))
-    up = cfg.costheta > 0
-    s11 = sm_rt["s11"].reshape(cfg.Nphi, cfg.Ntheta).T
-    assert np.all(s11[up] > 0)
-    assert abs(sum(energy.values()) - 1) < 1e-5
-    gs = M.SphereGeometry(R=2 * mie2.kl, scatterer=mie2)
-    cs = small_cfg(M, gs, 2000)
-    sm_rt, sm_cb, energy = M.run_rt(cs, gs)
-    assert np.all(np.isfinite(sm_rt["s11"])) and np.all(sm_rt["s11"] > 0)
+    if plane:
+        s11 = sm_rt["s11"].reshape(cfg.Nphi, cfg.Ntheta).T
+        assert np.all(s11[cfg.costheta > 0] > 0)
+        assert abs(sum(energy.values()) - 1) < 1e-9
+    else:
+        assert np.all(sm_rt["s11"] > 0)

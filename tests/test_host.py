@@ -137,10 +137,10 @@ def test_cpu_path_is_not_offered(M):
         M.simulate(M.Config(g), g, [1, 0, 0, 0], use_gpu=False)
 
 
-def _fake_simulate(calls):
-    """A stand-in for simulate() returning tallies that encode the incident state."""
+def _fake_sim(cfg, calls):
+    """A stand-in for one simulate() per incident state, with tallies that encode the state."""
 
-    def sim(cfg, g, I, **kw):
+    def sim(I, i):
         calls.append(np.array(I))
         k = len(calls)
         irt = np.zeros((4, cfg.Ntheta, cfg.Nphi))
@@ -153,16 +153,17 @@ def _fake_simulate(calls):
     return sim
 
 
-def test_run_rt_plane_assembly(M, monkeypatch):
-    """The plane Mueller assembly of MonteCarloRadiativeTransfer.jl:186-291."""
-    from mcrt_gb300 import engine
+def test_run_rt_plane_assembly_restatement(M):
+    """The checker's plane Mueller assembly (MonteCarloRadiativeTransfer.jl:186-291)
+    against hand-derived columns."""
+    from helpers import assemble_run_rt, table_of
 
-    calls = []
-    monkeypatch.setattr(engine, "simulate", _fake_simulate(calls))
     ray = M.RayleighScatterer(0.99, 1.0)
     g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0, scatterer=ray)])
     cfg = M.Config(g, Ntheta=4, Nphi=2, Nphib=2, thetab=[0.0, 0.1, math.pi / 2])
-    sm_rt, sm_cb, energy = M.run_rt(cfg, g)
+    calls = []
+    MRT, MCB, G = assemble_run_rt(cfg, g, _fake_sim(cfg, calls))
+    sm_rt, sm_cb = table_of(MRT, True), table_of(MCB, True)
     assert len(calls) == 6
     # column 1 = (R(-Q) + R(+Q)) / 2, column 2 = (R(+Q) - R(-Q)) / 2 of the raw tallies
     norm = np.abs(1 / (4 * cfg.costheta * cfg.inorm))
@@ -173,28 +174,53 @@ def test_run_rt_plane_assembly(M, monkeypatch):
     assert np.allclose(s12, (raw(2, 0) - raw(1, 0)) / 2 * norm[:, None])
     s44 = sm_rt["s44"].reshape(cfg.Nphi, cfg.Ntheta).T
     assert np.allclose(s44, (raw(6, 3) - raw(5, 3)) / 2 * norm[:, None])
-    assert np.allclose(sm_rt["theta"][: cfg.Ntheta], np.degrees(np.arccos(cfg.costheta)))
-    assert energy["direct_transmission"] == pytest.approx((0.1 + 0.2) / 2)
+    assert G[0] == pytest.approx((0.1 + 0.2) / 2)
     cb = sm_cb["s11"].reshape(cfg.Nphib, cfg.Nthetab).T
     rawb = lambda k, s: (s + 1) * 10.0 ** k + np.arange(cfg.Nthetab)[:, None]
     assert np.allclose(cb, (rawb(1, 0) + rawb(2, 0)) / 2 / np.abs(4 * cfg.costhetab)[:, None])
 
 
-def test_run_rt_sphere_assembly(M, monkeypatch):
-    """The sphere Mueller assembly of MonteCarloRadiativeTransfer.jl:87-184."""
-    from mcrt_gb300 import engine
+def test_run_rt_sphere_assembly_restatement(M):
+    """The checker's sphere Mueller assembly (MonteCarloRadiativeTransfer.jl:87-184)."""
+    from helpers import assemble_run_rt
 
-    calls = []
-    monkeypatch.setattr(engine, "simulate", _fake_simulate(calls))
     ray = M.RayleighScatterer(0.99, 1.0)
     g = M.SphereGeometry(R=1.0, scatterer=ray)
     cfg = M.Config(g, Ntheta=4, Nphi=8, Nphib=8, thetab=[0.0, 0.1])
-    sm_rt, sm_cb, energy = M.run_rt(cfg, g)
+    calls = []
+    MRT, MCB, G = assemble_run_rt(cfg, g, _fake_sim(cfg, calls))
     assert len(calls) == 2
     raw1 = lambda s, j2: (s + 1) * 10.0 + np.arange(cfg.Ntheta) + 0.1 * j2
     renorm = 1 / (0.1 + 0.3)
     exp11 = (raw1(0, 0) + raw1(0, 2) + raw1(0, 4) + raw1(0, 6)) * 0.25 * renorm / cfg.inorm
-    assert np.allclose(sm_rt["s11"], exp11)
+    assert np.allclose(MRT[0, 0], exp11)
     exp44 = -np.mean([(4 * 100.0 + np.arange(cfg.Ntheta) + 0.1 * j2) for j2 in range(8)], axis=0)
-    assert np.allclose(sm_rt["s44"], exp44 * renorm / cfg.inorm)
-    assert energy["reflection"] == pytest.approx(0.3)
+    assert np.allclose(MRT[3, 3], exp44 * renorm / cfg.inorm)
+    assert G[2] == pytest.approx(0.3)
+
+
+def test_run_rt_needs_a_device(M):
+    """run_rt has no CPU path: without a GPU it reports the missing device."""
+    L = M.lib()
+    if L.mcrt_device_count() > 0:
+        pytest.skip("a CUDA device is visible")
+    ray = M.RayleighScatterer(0.99, 1.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0, scatterer=ray)])
+    with pytest.raises(M.MCRTError):
+        M.run_rt(M.Config(g, number_of_rays=10), g)
+    with pytest.raises(NotImplementedError):
+        M.run_rt(M.Config(g, number_of_rays=10), g, use_gpu=False)
+
+
+def test_csv_writer_uses_the_reference_columns(M, tmp_path):
+    tab = {"theta": np.array([10.0, 20.0]), "phi": np.array([0.0, 0.0])}
+    for a in range(1, 5):
+        for b in range(1, 5):
+            tab[f"s{a}{b}"] = np.array([a + 0.1 * b, -(a + 0.1 * b)])
+    p = tmp_path / "rt.csv"
+    M.write_csv(tab, str(p))
+    lines = p.read_text(encoding="utf-8").splitlines()
+    head = lines[0].split(",")
+    assert head[:3] == ["θ", "ϕ", "s11"] and head[-1] == "s44" and len(head) == 18
+    row = [float(v) for v in lines[2].split(",")]
+    assert row[0] == 20.0 and row[2] == pytest.approx(-1.1) and row[-1] == pytest.approx(-4.4)
