@@ -33,12 +33,15 @@ sys.path.insert(0, os.path.join(ROOT, "montecarloradiativetransfer.jl_gb300"))
 
 WORKLOAD = "mie_x5_m1.5+0.001i_slab_tau5_zenith30"
 TOTAL_PHOTONS = 100_000_000
-# FP32 flops per bin evaluation of the persistent kernel's formulation, counted by
-# hand from csrc/mcrt_transport.cuh with FMA = 2 flops (SFU operations not counted):
-# RT peel-off bin with a Mie lookup, CB reciprocal-path bin, CB single-scattering bin.
-FLOPS_RT_MIE = 98.0
-FLOPS_CBN_MIE = 330.0
-FLOPS_CB1_MIE = 110.0
+# Algorithmic flops per bin evaluation of the reference's algorithm for a Mie
+# scatterer: additions + multiplications (FMA = 2), special functions (div, sqrt, exp,
+# sin/cos, acos) not counted. They come from the oracle's per-bin arithmetic
+# instantiated with an operation-counting scalar (oracle/opcount.cpp), and
+# tests/test_opcount.py checks these constants against it. Per RT peel-off bin, CB
+# reciprocal-path bin and CB single-scattering bin.
+FLOPS_RT_MIE = 128.349
+FLOPS_CBN_MIE = 409.0
+FLOPS_CB1_MIE = 196.0
 # DRAM bytes per launch of the transport kernel from ncu (scaled per photon from a
 # small capture); None until a capture has been summarised.
 NCU_DRAM_BYTES_PER_PHOTON = None

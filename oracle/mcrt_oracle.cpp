@@ -44,33 +44,64 @@
 
 namespace {
 
-using cplx = std::complex<double>;
 constexpr double PI = 3.14159265358979323846;
 constexpr double EPS = 2.220446049250313e-16;  // Julia eps(Float64)
 constexpr long MAX_ATTEMPTS = 1000000;
 constexpr int MAX_KEPLER = 100;  // same cap as the FP64 kernels
 
-struct V3 {
-  double x, y, z;
-};
-inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
-inline V3 operator*(double s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
-inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline double norm3(V3 a) { return std::sqrt(dot(a, a)); }
+// The per-bin arithmetic (frames, update_I, update_E, the bin bodies) is templated on
+// the scalar type R. The oracle instantiates it with double; opcount.cpp instantiates
+// it with an operation-counting type to fix the algorithmic flops per bin evaluation.
+// Elementary functions are called unqualified, so the counting type supplies its own.
+inline double Sqrt(double x) { return std::sqrt(x); }
+inline double Exp(double x) { return std::exp(x); }
+inline double Log(double x) { return std::log(x); }
+inline double Cos(double x) { return std::cos(x); }
+inline double Sin(double x) { return std::sin(x); }
+inline double Acos(double x) { return std::acos(x); }
+inline double Cbrt(double x) { return std::cbrt(x); }
+inline double Fabs(double x) { return std::fabs(x); }
+inline double Max(double a, double b) { return std::max(a, b); }
+inline long Trunc(double x) { return (long)std::trunc(x); }
 
-struct V4 {
-  double v[4];
+template <class R>
+struct V3T {
+  R x, y, z;
 };
-inline V4 scale4(V4 a, double s) { return {{a.v[0] * s, a.v[1] * s, a.v[2] * s, a.v[3] * s}}; }
+template <class R>
+inline V3T<R> operator+(V3T<R> a, V3T<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R>
+inline V3T<R> operator-(V3T<R> a, V3T<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R>
+inline V3T<R> operator-(V3T<R> a) { return {-a.x, -a.y, -a.z}; }
+template <class R>
+inline V3T<R> operator*(R s, V3T<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R>
+inline R dot(V3T<R> a, V3T<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R>
+inline R norm3(V3T<R> a) { return Sqrt(dot(a, a)); }
 
-struct Sph {
-  double ct, st, cp, sp;
+template <class R>
+struct V4T {
+  R v[4];
+};
+template <class R>
+inline V4T<R> scale4(V4T<R> a, R s) { return {{a.v[0] * s, a.v[1] * s, a.v[2] * s, a.v[3] * s}}; }
+
+template <class R>
+struct SphT {
+  R ct, st, cp, sp;
 };
 
-inline double jsign(double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0); }
-inline double clamp1(double c) { return c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c); }
+using V3 = V3T<double>;
+using V4 = V4T<double>;
+using Sph = SphT<double>;
+using cplx = std::complex<double>;
+
+template <class R>
+inline R jsign(R x) { return x > 0 ? R(1.0) : (x < 0 ? R(-1.0) : R(0.0)); }
+template <class R>
+inline R clamp1(R c) { return c > 1.0 ? R(1.0) : (c < -1.0 ? R(-1.0) : c); }
 
 // ---------------------------------------------------------------- Philox4x32-10
 // Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11.
@@ -117,46 +148,53 @@ struct Rng {
 
 // ---------------------------------------------------------------- frame algebra
 // utils.jl:9-23
-inline Sph spherical_from_cartesian(V3 x) {
-  double s2 = x.x * x.x + x.y * x.y;
-  if (s2 < 1e-24) return {jsign(x.z), 0.0, 1.0, 0.0};
-  double ct = clamp1(x.z);
-  double st = std::sqrt(1.0 - ct * ct);
-  double si = 1.0 / std::sqrt(s2);
+template <class R>
+inline SphT<R> spherical_from_cartesian(V3T<R> x) {
+  R s2 = x.x * x.x + x.y * x.y;
+  if (s2 < 1e-24) return {jsign(x.z), R(0.0), R(1.0), R(0.0)};
+  R ct = clamp1(x.z);
+  R st = Sqrt(R(1.0) - ct * ct);
+  R si = R(1.0) / Sqrt(s2);
   return {ct, st, x.x * si, x.y * si};
 }
 
 // utils.jl:30-34
-inline V3 ray_to_norm(V3 x, double ct, double st, double cp, double sp) {
+template <class R>
+inline V3T<R> ray_to_norm(V3T<R> x, R ct, R st, R cp, R sp) {
   return {x.x * ct * cp - x.y * sp + x.z * st * cp, x.x * ct * sp + x.y * cp + x.z * st * sp,
           -x.x * st + x.z * ct};
 }
-inline V3 ray_to_norm(V3 x, const Sph& s) { return ray_to_norm(x, s.ct, s.st, s.cp, s.sp); }
+template <class R>
+inline V3T<R> ray_to_norm(V3T<R> x, const SphT<R>& s) { return ray_to_norm(x, s.ct, s.st, s.cp, s.sp); }
 
 // utils.jl:41-45
-inline V3 norm_to_ray(V3 x, double ct, double st, double cp, double sp) {
+template <class R>
+inline V3T<R> norm_to_ray(V3T<R> x, R ct, R st, R cp, R sp) {
   return {x.x * ct * cp + x.y * ct * sp - x.z * st, -x.x * sp + x.y * cp,
           x.x * st * cp + x.y * st * sp + x.z * ct};
 }
-inline V3 norm_to_ray(V3 x, const Sph& s) { return norm_to_ray(x, s.ct, s.st, s.cp, s.sp); }
+template <class R>
+inline V3T<R> norm_to_ray(V3T<R> x, const SphT<R>& s) { return norm_to_ray(x, s.ct, s.st, s.cp, s.sp); }
 
 // utils.jl:52-62 (the y component of Ev keeps the reference's sign, utils.jl:60)
-inline void get_basis(V3 k, V3& Eh, V3& Ev) {
-  if (std::fabs(k.z) > 1.0 - EPS) {
-    Eh = {0.0, -1.0, 0.0};
-    Ev = {jsign(k.z), 0.0, 0.0};
+template <class R>
+inline void get_basis(V3T<R> k, V3T<R>& Eh, V3T<R>& Ev) {
+  if (Fabs(k.z) > 1.0 - EPS) {
+    Eh = {R(0.0), R(-1.0), R(0.0)};
+    Ev = {jsign(k.z), R(0.0), R(0.0)};
   } else {
-    double ev3 = -std::sqrt(1.0 - k.z * k.z);
-    double inv = 1.0 / ev3;
-    double eh1 = k.y * -inv;
-    double eh2 = k.x * inv;
-    Eh = {eh1, eh2, 0.0};
+    R ev3 = -Sqrt(R(1.0) - k.z * k.z);
+    R inv = R(1.0) / ev3;
+    R eh1 = k.y * -inv;
+    R eh2 = k.x * inv;
+    Eh = {eh1, eh2, R(0.0)};
     Ev = {-k.z * eh2, -k.z * eh1, ev3};
   }
 }
 
 // utils.jl:82-84
-inline V4 rotate(V4 I, double c2, double s2) {
+template <class R>
+inline V4T<R> rotate(V4T<R> I, R c2, R s2) {
   return {{I.v[0], c2 * I.v[1] + s2 * I.v[2], -s2 * I.v[1] + c2 * I.v[2], I.v[3]}};
 }
 
@@ -169,35 +207,38 @@ struct Scat {
   std::vector<cplx> S11, S22;
 };
 
-struct PM {  // phase matrix in the reference's block form
-  double p11, p12, p33, p34;
+template <class R>
+struct PMT {  // phase matrix in the reference's block form
+  R p11, p12, p33, p34;
 };
+using PM = PMT<double>;
 
 // rayleigh.jl:8-18 and mie.jl:46-74; u < 0 means "do not sample" (cos given).
-inline PM phase_matrix(const Scat& s, double& c, double u, bool sample) {
+template <class R>
+inline PMT<R> phase_matrix(const Scat& s, R& c, R u, bool sample) {
   if (s.kind == 0) {
     if (sample) {
-      double rn = 2.0 * (1.0 - 2.0 * u);
-      double r = std::sqrt(1.0 + rn * rn);
-      c = std::cbrt(r + rn) - std::cbrt(r - rn);
+      R rn = 2.0 * (1.0 - 2.0 * u);
+      R r = Sqrt(1.0 + rn * rn);
+      c = Cbrt(r + rn) - Cbrt(r - rn);
     }
-    double c2 = c * c;
-    return {0.75 * (1 + c2), -0.75 * (1 - c2), 1.5 * c, 0.0};
+    R c2 = c * c;
+    return {0.75 * (1 + c2), -0.75 * (1 - c2), 1.5 * c, R(0.0)};
   }
   if (sample) {
-    double rn = u * s.random_points;
-    long mrn = (long)std::trunc(rn);
+    R rn = u * (double)s.random_points;
+    long mrn = Trunc(rn);
     if (mrn > s.random_points - 1) mrn = s.random_points - 1;
-    c = (mrn + 1 - rn) * s.csrn[mrn] + (rn - mrn) * s.csrn[mrn + 1];
+    c = ((double)(mrn + 1) - rn) * s.csrn[mrn] + (rn - (double)mrn) * s.csrn[mrn + 1];
   }
-  double th = std::acos(clamp1(c));
-  double sn = th / PI * (s.ntheta - 1);
-  long msn = (long)std::trunc(sn) + 1;  // 1-based as in mie.jl:55
+  R th = Acos(clamp1(c));
+  R sn = th / PI * (double)(s.ntheta - 1);
+  long msn = Trunc(sn) + 1;  // 1-based as in mie.jl:55
   if (msn > s.ntheta) msn = s.ntheta;
-  double w0 = msn - sn;
-  PM p{w0 * s.F11[msn - 1], w0 * s.F12[msn - 1], w0 * s.F33[msn - 1], w0 * s.F34[msn - 1]};
+  R w0 = (double)msn - sn;
+  PMT<R> p{w0 * s.F11[msn - 1], w0 * s.F12[msn - 1], w0 * s.F33[msn - 1], w0 * s.F34[msn - 1]};
   if (msn + 1 <= s.ntheta) {
-    double w1 = sn - msn + 1;
+    R w1 = sn - (double)msn + 1.0;
     p.p11 += w1 * s.F11[msn];
     p.p12 += w1 * s.F12[msn];
     p.p33 += w1 * s.F33[msn];
@@ -206,103 +247,110 @@ inline PM phase_matrix(const Scat& s, double& c, double u, bool sample) {
   return p;
 }
 
-inline V4 pm_apply(const PM& p, V4 I) {
+template <class R>
+inline V4T<R> pm_apply(const PMT<R>& p, V4T<R> I) {
   return {{p.p11 * I.v[0] + p.p12 * I.v[1], p.p12 * I.v[0] + p.p11 * I.v[1],
            p.p33 * I.v[2] + p.p34 * I.v[3], -p.p34 * I.v[2] + p.p33 * I.v[3]}};
 }
 
 // rayleigh.jl:20-23 and mie.jl:76-92 (keeps the (2-f, f-1) weights of mie.jl:80-85)
-inline void amplitude_matrix(const Scat& s, double c, cplx& S11, cplx& S22) {
+template <class R>
+inline void amplitude_matrix(const Scat& s, R c, std::complex<R>& S11, std::complex<R>& S22) {
+  using C = std::complex<R>;
   if (s.kind == 0) {
-    S11 = cplx(0.0, 1.0);
-    S22 = cplx(0.0, c);
+    S11 = C(R(0.0), R(1.0));
+    S22 = C(R(0.0), c);
     return;
   }
-  double th = std::acos(clamp1(c));
-  double sn = th / PI * (s.ntheta - 1);
-  long msn = (long)std::trunc(sn) + 1;
+  R th = Acos(clamp1(c));
+  R sn = th / PI * (double)(s.ntheta - 1);
+  long msn = Trunc(sn) + 1;
   if (msn > s.ntheta) msn = s.ntheta;
-  double w0 = msn + 1 - sn;
-  S11 = w0 * s.S11[msn - 1];
-  S22 = w0 * s.S22[msn - 1];
+  R w0 = (double)(msn + 1) - sn;
+  S11 = w0 * C(R(s.S11[msn - 1].real()), R(s.S11[msn - 1].imag()));
+  S22 = w0 * C(R(s.S22[msn - 1].real()), R(s.S22[msn - 1].imag()));
   if (msn + 1 <= s.ntheta) {
-    double w1 = sn - msn;
-    S11 += w1 * s.S11[msn];
-    S22 += w1 * s.S22[msn];
+    R w1 = sn - (double)msn;
+    S11 += w1 * C(R(s.S11[msn].real()), R(s.S11[msn].imag()));
+    S22 += w1 * C(R(s.S22[msn].real()), R(s.S22[msn].imag()));
   }
 }
 
 // utils.jl:91-112
-inline V4 update_I(const Scat& sca, V4 I, V3 k, const Sph& f, V3* Eh_out = nullptr,
-                   V3* Ev_out = nullptr) {
-  V3 Eh, Ev;
+template <class R>
+inline V4T<R> update_I(const Scat& sca, V4T<R> I, V3T<R> k, const SphT<R>& f, V3T<R>* Eh_out = nullptr,
+                       V3T<R>* Ev_out = nullptr) {
+  V3T<R> Eh, Ev;
   get_basis(k, Eh, Ev);
-  V3 kr = norm_to_ray(k, f);
-  Sph ks = spherical_from_cartesian(kr);
-  V3 Ehk = ray_to_norm(V3{ks.sp, -ks.cp, 0.0}, f);
-  V3 Evk = ray_to_norm(V3{ks.ct * ks.cp, ks.ct * ks.sp, -ks.st}, f);
-  double cpsi = Eh.x * Ehk.x + Eh.y * Ehk.y;
-  double spsi = -Eh.x * Evk.x - Eh.y * Evk.y;
-  double c = std::max(kr.z, -1.0);
-  PM P = phase_matrix(sca, c, 0.0, false);
-  V4 Ip = pm_apply(P, rotate(I, ks.cp * ks.cp - ks.sp * ks.sp, -2 * ks.sp * ks.cp));
-  Ip = rotate(Ip, cpsi * cpsi - spsi * spsi, 2 * spsi * cpsi);
+  V3T<R> kr = norm_to_ray(k, f);
+  SphT<R> ks = spherical_from_cartesian(kr);
+  V3T<R> Ehk = ray_to_norm(V3T<R>{ks.sp, -ks.cp, R(0.0)}, f);
+  V3T<R> Evk = ray_to_norm(V3T<R>{ks.ct * ks.cp, ks.ct * ks.sp, -ks.st}, f);
+  R cpsi = Eh.x * Ehk.x + Eh.y * Ehk.y;
+  R spsi = -Eh.x * Evk.x - Eh.y * Evk.y;
+  R c = Max(kr.z, R(-1.0));
+  PMT<R> P = phase_matrix(sca, c, R(0.0), false);
+  V4T<R> Ip = pm_apply(P, rotate(I, ks.cp * ks.cp - ks.sp * ks.sp, -2.0 * ks.sp * ks.cp));
+  Ip = rotate(Ip, cpsi * cpsi - spsi * spsi, 2.0 * spsi * cpsi);
   if (Eh_out) *Eh_out = Eh;
   if (Ev_out) *Ev_out = Ev;
   return Ip;
 }
 
 // utils.jl:119-150
-inline void E_from_I(V4 I, cplx& E1, cplx& E2) {
+template <class R>
+inline void E_from_I(V4T<R> I, std::complex<R>& E1, std::complex<R>& E2) {
   const double tol = 1e-14;
-  double A1, A2, phi2;
-  if (I.v[0] - std::fabs(I.v[1]) > tol * I.v[0]) {
-    A1 = std::sqrt(0.5 * (I.v[0] - I.v[1]));
-    A2 = std::sqrt(0.5 * (I.v[0] + I.v[1]));
-    double q = std::sqrt(I.v[0] * I.v[0] - I.v[1] * I.v[1]);
+  R A1, A2, phi2;
+  if (I.v[0] - Fabs(I.v[1]) > tol * I.v[0]) {
+    A1 = Sqrt(0.5 * (I.v[0] - I.v[1]));
+    A2 = Sqrt(0.5 * (I.v[0] + I.v[1]));
+    R q = Sqrt(I.v[0] * I.v[0] - I.v[1] * I.v[1]);
     if (I.v[2] >= q) {
       phi2 = 0.0;
     } else if (I.v[2] <= -q) {
       phi2 = PI;
     } else {
-      phi2 = std::acos(I.v[2] / q);
+      phi2 = Acos(I.v[2] / q);
       if (I.v[3] > 0.0) phi2 = 2 * PI - phi2;
     }
   } else if (I.v[0] + I.v[1] <= tol * I.v[0]) {
-    A1 = std::sqrt(I.v[0]);
+    A1 = Sqrt(I.v[0]);
     A2 = 0.0;
     phi2 = 0.0;
   } else {
     A1 = 0.0;
-    A2 = std::sqrt(I.v[0]);
+    A2 = Sqrt(I.v[0]);
     phi2 = 0.0;
   }
-  E1 = cplx(A1, 0.0);
-  E2 = A2 * cplx(std::cos(phi2), std::sin(phi2));
+  E1 = std::complex<R>(A1, R(0.0));
+  E2 = A2 * std::complex<R>(Cos(phi2), Sin(phi2));
 }
 
 // utils.jl:157-163
-inline V4 I_from_E(cplx E1, cplx E2) {
-  double qh = E1.real() * E1.real() + E1.imag() * E1.imag();
-  double qv = E2.real() * E2.real() + E2.imag() * E2.imag();
-  cplx x = E2 * std::conj(E1);
+template <class R>
+inline V4T<R> I_from_E(std::complex<R> E1, std::complex<R> E2) {
+  R qh = E1.real() * E1.real() + E1.imag() * E1.imag();
+  R qv = E2.real() * E2.real() + E2.imag() * E2.imag();
+  std::complex<R> x = E2 * std::conj(E1);
   return {{qh + qv, -qh + qv, 2.0 * x.real(), -2.0 * x.imag()}};
 }
 
 // utils.jl:170-192
-inline void update_E(const Scat& sca, cplx& E1, cplx& E2, V3 k, const Sph& f, V3* Eh_out = nullptr,
-                     V3* Ev_out = nullptr) {
-  V3 Eh, Ev;
+template <class R>
+inline void update_E(const Scat& sca, std::complex<R>& E1, std::complex<R>& E2, V3T<R> k, const SphT<R>& f,
+                     V3T<R>* Eh_out = nullptr, V3T<R>* Ev_out = nullptr) {
+  V3T<R> Eh, Ev;
   get_basis(k, Eh, Ev);
-  V3 kr = norm_to_ray(k, f);
-  Sph ks = spherical_from_cartesian(kr);
-  V3 Ehk = ray_to_norm(V3{ks.sp, -ks.cp, 0.0}, f);
-  V3 Evk = ray_to_norm(V3{ks.ct * ks.cp, ks.ct * ks.sp, -ks.st}, f);
-  double cpsi = Eh.x * Ehk.x + Eh.y * Ehk.y;
-  double spsi = Eh.x * Evk.x + Eh.y * Evk.y;
-  cplx S11, S22;
+  V3T<R> kr = norm_to_ray(k, f);
+  SphT<R> ks = spherical_from_cartesian(kr);
+  V3T<R> Ehk = ray_to_norm(V3T<R>{ks.sp, -ks.cp, R(0.0)}, f);
+  V3T<R> Evk = ray_to_norm(V3T<R>{ks.ct * ks.cp, ks.ct * ks.sp, -ks.st}, f);
+  R cpsi = Eh.x * Ehk.x + Eh.y * Ehk.y;
+  R spsi = Eh.x * Evk.x + Eh.y * Evk.y;
+  std::complex<R> S11, S22;
   amplitude_matrix(sca, kr.z, S11, S22);
-  cplx a = E1 * ks.cp + E2 * ks.sp, b = -E1 * ks.sp + E2 * ks.cp;
+  std::complex<R> a = E1 * ks.cp + E2 * ks.sp, b = -E1 * ks.sp + E2 * ks.cp;
   a = S11 * a;
   b = S22 * b;
   E1 = a * cpsi + b * spsi;
@@ -348,14 +396,16 @@ struct Geom {
   int nl() const { return (int)layers.size(); }
 };
 
-inline double distance_to_boundary(const Geom& g, V3 x, V3 k, int idx) {
+template <class R>
+inline R distance_to_boundary(const Geom& g, V3T<R> x, V3T<R> k, int idx) {
   if (g.kind == 0) {  // plane.jl:97-105
     if (k.z > 0) return -x.z / k.z;
     if (!g.layers[idx].inf) return (x.z + g.layers[idx].tau) / -k.z;
-    return INFINITY;
+    return R(INFINITY);
   }
-  double kx = dot(k, x), xx = dot(x, x), tau = g.layers[0].tau;  // sphere.jl:69-73
-  return -kx + std::sqrt(std::max(kx * kx + tau * tau - xx, 0.0));
+  R kx = dot(k, x), xx = dot(x, x);  // sphere.jl:69-73
+  double tau = g.layers[0].tau;
+  return -kx + Sqrt(Max(kx * kx + tau * tau - xx, R(0.0)));
 }
 
 inline int pass_boundary(const Geom& g, V3 x, int idx) {
@@ -450,6 +500,21 @@ inline V4 scatter(const Ctx& C, V4 I, V3 k, int idx, double u0, double u1, V3& k
   return scale4(Ip, I.v[0] / Ip.v[0]);
 }
 
+// One RT bin of cpu.jl:13-26: the peel-off Stokes vector into the direction
+// (st cos(phi), st sin(phi), ct) with its attenuation and quadrature weight. Returns
+// false when the path to the boundary is longer than tau0 (no contribution).
+template <class R>
+inline bool rt_bin(const Scat& sca, const Geom& g, double tau0, V4T<R> I, const SphT<R>& ks, V3T<R> x, int idx,
+                   R st, R ct, R cphi, R sphi, R inorm, V4T<R>& Ipp) {
+  V3T<R> kk{st * cphi, st * sphi, ct};
+  V4T<R> Ip = update_I(sca, I, kk, ks);
+  R t = distance_to_boundary(g, x, kk, idx);
+  if (!(t <= tau0)) return false;
+  R nx = Exp(-t);
+  Ipp = scale4(Ip, inorm * nx);
+  return true;
+}
+
 // cpu.jl:6-31
 inline double collect_rt(const Ctx& C, Tally& T, V4 I, V3 k, V3 x, int idx, int j1a, int j1b) {
   const Cfg& cfg = *C.cfg;
@@ -458,12 +523,9 @@ inline double collect_rt(const Ctx& C, Tally& T, V4 I, V3 k, V3 x, int idx, int 
   double acc = 0.0;
   for (int j2 = 0; j2 < cfg.nphi; ++j2) {
     for (int j1 = j1a; j1 < j1b; ++j1) {
-      V3 kk{cfg.stheta[j1] * cfg.cphi[j2], cfg.stheta[j1] * cfg.sphi[j2], cfg.ctheta[j1]};
-      V4 Ip = update_I(sca, I, kk, ks);
-      double t = distance_to_boundary(*C.g, x, kk, idx);
-      if (t <= cfg.tau0) {
-        double nx = std::exp(-t);
-        V4 Ipp = scale4(Ip, cfg.inorm[j1] * nx);
+      V4 Ipp;
+      if (rt_bin(sca, *C.g, cfg.tau0, I, ks, x, idx, cfg.stheta[j1], cfg.ctheta[j1], cfg.cphi[j2], cfg.sphi[j2],
+                 cfg.inorm[j1], Ipp)) {
         double* dst = &T.Irt[4 * ((size_t)j2 * cfg.ntheta + j1)];
         for (int s = 0; s < 4; ++s) dst[s] += Ipp.v[s];
         acc += Ipp.v[0];
@@ -534,6 +596,76 @@ struct PathBuf {
   std::vector<int> idxpath;
 };
 
+// Per-event inputs of one reciprocal-path CB bin (computed once per event, cpu.jl:42-81).
+template <class R>
+struct CBNIn {
+  SphT<R> kfs, kas, kbs;
+  V3T<R> ki, xa, xb;
+  int idxa, idxb;
+  R kl, tab;
+  std::complex<R> Ea1, Ea2, Eb1, Eb2;
+};
+
+// One reciprocal-path CB bin of cpu.jl:85-126: the forward and backward fields into the
+// bin direction, their attenuations, the interference with phase kl (ki + kf).(xa - xb),
+// and the rotation into the bin's frame. Returns false when tau0 cuts the forward path.
+template <class R>
+inline bool cbn_bin(const Scat& sca, const Geom& g, double tau0, const CBNIn<R>& e, R stb, R ctb, R cpb, R spb,
+                    V4T<R>& I1, R& ladder) {
+  V3T<R> kfb{stb * cpb, stb * spb, ctb};
+  kfb = ray_to_norm(kfb, e.kfs);
+  std::complex<R> a1 = e.Ea1, a2 = e.Ea2, b1 = e.Eb1, b2 = e.Eb2;
+  update_E(sca, a1, a2, kfb, e.kas);
+  V3T<R> Eh, Ev;
+  update_E(sca, b1, b2, kfb, e.kbs, &Eh, &Ev);
+  R dphi = e.kl * dot(e.ki + kfb, e.xa - e.xb);
+  R tya = distance_to_boundary(g, e.xa, kfb, e.idxa);
+  if (!(tya <= tau0)) return false;
+  R nexta = Exp(-0.5 * tya);
+  a1 *= nexta;
+  a2 *= nexta;
+  V4T<R> Ia = I_from_E(a1, a2);
+  R tyb = distance_to_boundary(g, e.xb, kfb, e.idxb);
+  if (Fabs(tyb + e.tab) <= tau0) {
+    R nextb = Exp(-0.5 * (tyb + e.tab));
+    b1 *= nextb;
+    b2 *= nextb;
+  } else {
+    b1 = R(0.0);
+    b2 = R(0.0);
+  }
+  V4T<R> Ib = I_from_E(b1, b2);
+  std::complex<R> ph(Cos(dphi), Sin(dphi));
+  V4T<R> Iab = I_from_E(a1 * ph + b1, a2 * ph + b2);
+  Iab = scale4(Iab, Ia.v[0] / (Ia.v[0] + Ib.v[0]));
+  Eh = norm_to_ray(Eh, e.kfs);
+  Ev = norm_to_ray(Ev, e.kfs);
+  R cpsi = spb * Eh.x - cpb * Eh.y;
+  R spsi = -spb * Ev.x + cpb * Ev.y;
+  I1 = rotate(Iab, cpsi * cpsi - spsi * spsi, 2.0 * cpsi * spsi);
+  ladder = Ia.v[0];
+  return true;
+}
+
+// One single-scattering CB bin of cpu.jl:132-156.
+template <class R>
+inline bool cb1_bin(const Scat& sca, const Geom& g, double tau0, V4T<R> I, const SphT<R>& kfs, const SphT<R>& kas,
+                    V3T<R> xa, int idxa, R stb, R ctb, R cpb, R spb, V4T<R>& I1) {
+  V3T<R> kfb{stb * cpb, stb * spb, ctb};
+  kfb = ray_to_norm(kfb, kfs);
+  V3T<R> Eh, Ev;
+  V4T<R> Iaf = update_I(sca, I, kfb, kas, &Eh, &Ev);
+  R tya = distance_to_boundary(g, xa, kfb, idxa);
+  if (!(tya <= tau0)) return false;
+  Iaf = scale4(Iaf, Exp(-tya));
+  Eh = norm_to_ray(Eh, kfs);
+  Ev = norm_to_ray(Ev, kfs);
+  R cpsi = spb * Eh.x - cpb * Eh.y;
+  R spsi = -spb * Ev.x + cpb * Ev.y;
+  I1 = rotate(Iaf, cpsi * cpsi - spsi * spsi, 2.0 * cpsi * spsi);
+  return true;
+}
+
 // cpu.jl:38-160, plus the ladder (incoherent) s11 and the per-photon CB-peak value.
 inline void collect_cb(const Ctx& C, Tally& T, V4 I, V3 k, V3 x, int idx, const PathBuf& pb, int n,
                        const CBState* inc, double& peak) {
@@ -590,42 +722,15 @@ inline void collect_cb(const Ctx& C, Tally& T, V4 I, V3 k, V3 x, int idx, const 
     Ea2 *= raa;
     Eb1 *= raa;
     Eb2 *= raa;
+    const CBNIn<double> e{kfs, kas, kbs, ki, xa, xb, idxa, idxb, kl, tab, Ea1, Ea2, Eb1, Eb2};
     for (int j2 = 0; j2 < cfg.nphib; ++j2) {
       for (int j1 = 0; j1 < cfg.nthetab; ++j1) {
-        V3 kfb{cfg.sthetab[j1] * cfg.cphib[j2], cfg.sthetab[j1] * cfg.sphib[j2], cfg.cthetab[j1]};
-        kfb = ray_to_norm(kfb, kfs);
-        cplx a1 = Ea1, a2 = Ea2, b1 = Eb1, b2 = Eb2;
-        update_E(sca, a1, a2, kfb, kas);
-        V3 Eh, Ev;
-        update_E(sca, b1, b2, kfb, kbs, &Eh, &Ev);
-        double dphi = kl * dot(ki + kfb, xa - xb);
-        double tya = distance_to_boundary(g, xa, kfb, idxa);
-        if (tya <= cfg.tau0) {
-          double nexta = std::exp(-0.5 * tya);
-          a1 *= nexta;
-          a2 *= nexta;
-          V4 Ia = I_from_E(a1, a2);
-          double tyb = distance_to_boundary(g, xb, kfb, idxb);
-          if (std::fabs(tyb + tab) <= cfg.tau0) {
-            double nextb = std::exp(-0.5 * (tyb + tab));
-            b1 *= nextb;
-            b2 *= nextb;
-          } else {
-            b1 = 0.0;
-            b2 = 0.0;
-          }
-          V4 Ib = I_from_E(b1, b2);
-          cplx ph(std::cos(dphi), std::sin(dphi));
-          V4 Iab = I_from_E(a1 * ph + b1, a2 * ph + b2);
-          Iab = scale4(Iab, Ia.v[0] / (Ia.v[0] + Ib.v[0]));
-          Eh = norm_to_ray(Eh, kfs);
-          Ev = norm_to_ray(Ev, kfs);
-          double cpsi = cfg.sphib[j2] * Eh.x - cfg.cphib[j2] * Eh.y;
-          double spsi = -cfg.sphib[j2] * Ev.x + cfg.cphib[j2] * Ev.y;
-          V4 I1 = rotate(Iab, cpsi * cpsi - spsi * spsi, 2.0 * cpsi * spsi);
+        V4 I1;
+        double lad;
+        if (cbn_bin(sca, g, cfg.tau0, e, cfg.sthetab[j1], cfg.cthetab[j1], cfg.cphib[j2], cfg.sphib[j2], I1, lad)) {
           size_t b = (size_t)j2 * cfg.nthetab + j1;
           for (int s = 0; s < 4; ++s) T.Icb[4 * b + s] += I1.v[s];
-          T.ladder[b] += Ia.v[0];
+          T.ladder[b] += lad;
           if (b == 0) peak += I1.v[0];
         }
       }
@@ -634,18 +739,9 @@ inline void collect_cb(const Ctx& C, Tally& T, V4 I, V3 k, V3 x, int idx, const 
   } else {
     for (int j2 = 0; j2 < cfg.nphib; ++j2) {
       for (int j1 = 0; j1 < cfg.nthetab; ++j1) {
-        V3 kfb{cfg.sthetab[j1] * cfg.cphib[j2], cfg.sthetab[j1] * cfg.sphib[j2], cfg.cthetab[j1]};
-        kfb = ray_to_norm(kfb, kfs);
-        V3 Eh, Ev;
-        V4 Iaf = update_I(sca, I, kfb, kas, &Eh, &Ev);
-        double tya = distance_to_boundary(g, xa, kfb, idxa);
-        if (tya <= cfg.tau0) {
-          Iaf = scale4(Iaf, std::exp(-tya));
-          Eh = norm_to_ray(Eh, kfs);
-          Ev = norm_to_ray(Ev, kfs);
-          double cpsi = cfg.sphib[j2] * Eh.x - cfg.cphib[j2] * Eh.y;
-          double spsi = -cfg.sphib[j2] * Ev.x + cfg.cphib[j2] * Ev.y;
-          V4 I1 = rotate(Iaf, cpsi * cpsi - spsi * spsi, 2.0 * cpsi * spsi);
+        V4 I1;
+        if (cb1_bin(sca, g, cfg.tau0, I, kfs, kas, xa, idxa, cfg.sthetab[j1], cfg.cthetab[j1], cfg.cphib[j2],
+                    cfg.sphib[j2], I1)) {
           size_t b = (size_t)j2 * cfg.nthetab + j1;
           for (int s = 0; s < 4; ++s) T.Icb[4 * b + s] += I1.v[s];
           T.ladder[b] += I1.v[0];
