@@ -160,6 +160,9 @@ int mcrt_ctx_destroy(mcrt_ctx* ctx);
  * src/MonteCarloRadiativeTransfer.jl:92-99,194-199). */
 int mcrt_scatterer_create(mcrt_ctx* ctx, const mcrt_scatterer_desc* desc, mcrt_scatterer** out);
 int mcrt_scatterer_destroy(mcrt_scatterer* s);
+/* Single-scattering albedo and mean free path of a scatterer (for scatterers whose
+ * tables were made on the device). */
+int mcrt_scatterer_params(const mcrt_scatterer* s, double* omega, double* kl);
 
 /* Host-side table producer for MieScatterer(r, m, lambda, nu; Ntheta, random_points)
  * (src/scatterers/mie.jl:36-44, bhmie :129-216, calculate_csrn src/utils.jl:263-287).
@@ -168,6 +171,17 @@ int mcrt_scatterer_destroy(mcrt_scatterer* s);
 int mcrt_mie_tables(double r, double m_re, double m_im, double lambda, double nu, int n_theta,
                     int random_points, double* omega, double* kl, double* F11, double* F12,
                     double* F33, double* F34, double* S11, double* S22, double* csrn, double* q);
+
+/* The same table producer on the device, for n scatterers in one launch (one thread
+ * block each): MieScatterer(r[i], m_re[i] + i m_im[i], lambda[i], nu[i]; n_theta,
+ * random_points) becomes out[i], a scatterer whose FP32 tables are written on the
+ * device and never pass through host memory (for a serving stream in which requests
+ * bring new size parameters and refractive indices). tables (optional, host) receives
+ * per scatterer 7 + 8*n_theta + random_points + 1 doubles: omega, kl, q[5] (as in
+ * mcrt_mie_tables), F11, F12, F33, F34, S11 (re/im), S22 (re/im), csrn. */
+int mcrt_mie_scatterers_create(mcrt_ctx* ctx, int n, const double* r, const double* m_re, const double* m_im,
+                               const double* lambda, const double* nu, int n_theta, int random_points,
+                               mcrt_scatterer** out, double* tables);
 
 /* ------------------------------------------------------------------ simulate */
 /* The drop-in for simulate(cfg, g, I0; use_gpu=true): runs cfg.number_of_rays photons

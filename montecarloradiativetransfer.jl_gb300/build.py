@@ -28,7 +28,7 @@ NVCC_FLAGS = ARCH + [
     "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr",
 ]
 # Each unit instantiates a subset of the kernels so that they compile in parallel.
-UNITS = ["mcrt_api.cu", "mcrt_k_fp32.cu", "mcrt_k_fp64.cu", "mcrt_k_plain.cu", "mcrt_server.cu"]
+UNITS = ["mcrt_api.cu", "mcrt_k_fp32.cu", "mcrt_k_fp64.cu", "mcrt_k_plain.cu", "mcrt_mie.cu"]
 
 
 def _nvcc() -> str:

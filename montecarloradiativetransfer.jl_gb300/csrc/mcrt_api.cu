@@ -20,6 +20,7 @@
 #include "mcrt_device.cuh"
 #include "mcrt_host.h"
 #include "mcrt_kernels.h"
+#include "mcrt_mie.cuh"
 
 using namespace mcrt;
 
@@ -190,6 +191,13 @@ int mcrt_scatterer_create(mcrt_ctx* ctx, const mcrt_scatterer_desc* d, mcrt_scat
   return MCRT_OK;
 }
 
+int mcrt_scatterer_params(const mcrt_scatterer* s, double* omega, double* kl) {
+  if (!s) return set_err(MCRT_EINVAL, "mcrt_scatterer_params: NULL scatterer");
+  if (omega) *omega = s->omega;
+  if (kl) *kl = s->kl;
+  return MCRT_OK;
+}
+
 int mcrt_scatterer_destroy(mcrt_scatterer* s) {
   if (!s) return MCRT_OK;
   cudaSetDevice(s->ctx->device);
@@ -231,6 +239,84 @@ int mcrt_mie_tables(double r, double m_re, double m_im, double lambda, double nu
     q[3] = R.q_back;
     q[4] = R.asymm;
   }
+  return MCRT_OK;
+}
+
+int mcrt_mie_scatterers_create(mcrt_ctx* ctx, int n, const double* r, const double* m_re, const double* m_im,
+                               const double* lambda, const double* nu, int n_theta, int random_points,
+                               mcrt_scatterer** out, double* tables) {
+  if (!ctx || n < 1 || !r || !m_re || !m_im || !lambda || !nu || !out)
+    return set_err(MCRT_EINVAL, "mcrt_mie_scatterers_create: bad argument");
+  if (n_theta < 2 || random_points < 1)
+    return set_err(MCRT_EINVAL, "mcrt_mie_scatterers_create: need n_theta >= 2 and random_points >= 1");
+  for (int i = 0; i < n; ++i) {
+    out[i] = nullptr;
+    if (!(r[i] > 0) || !(lambda[i] > 0) || !(nu[i] > 0) || !std::isfinite(m_re[i]) || !std::isfinite(m_im[i]))
+      return set_err(MCRT_EINVAL, "mcrt_mie_scatterers_create: need r, lambda, nu > 0 and a finite m");
+  }
+  CK(cudaSetDevice(ctx->device));
+  const size_t nres = mie_result_doubles(n_theta, random_points);
+  std::vector<MieJob> jobs(n);
+  std::vector<size_t> scratch_off(n);
+  size_t scratch = 0;
+  for (int i = 0; i < n; ++i) {
+    MieJob& J = jobs[i];
+    J.x = 2 * host::PI * r[i] / lambda[i];  // mie.jl:37
+    J.m_re = m_re[i];
+    J.m_im = m_im[i];
+    J.r = r[i];
+    J.nu = nu[i];
+    J.nt = n_theta;
+    J.rp = random_points;
+    // the series length of bhmie (mie.jl:133-135), computed on the host as there
+    J.nstop = (int)std::floor(std::max(J.x + 4 * std::cbrt(J.x) + 2, J.x * std::hypot(m_re[i], m_im[i])));
+    J.nmax = J.nstop + 15;
+    if (J.nstop < 1 || J.nstop > (1 << 20))
+      return set_err(MCRT_EINVAL, "mcrt_mie_scatterers_create: size parameter out of range");
+    scratch_off[i] = scratch;
+    scratch += 2 * (size_t)(J.nmax + 1) + 4 * (size_t)(J.nstop + 1) + 2 * (size_t)(random_points + 1);
+    J.nc = ((random_points + 2 + 3) / 4) * 4;
+  }
+  DevBuf d_scr, d_res, d_jobs;
+  CK(d_scr.alloc(scratch * sizeof(double)));
+  CK(d_res.alloc(nres * n * sizeof(double)));
+  std::vector<std::unique_ptr<mcrt_scatterer>> made(n);
+  for (int i = 0; i < n; ++i) {
+    MieJob& J = jobs[i];
+    made[i].reset(new mcrt_scatterer());
+    mcrt_scatterer& s = *made[i];
+    s.ctx = ctx;
+    s.kind = MCRT_MIE;
+    s.ntheta = n_theta;
+    s.rp = random_points;
+    CK(s.F.alloc((n_theta + 1) * sizeof(float4)));
+    CK(s.S.alloc((n_theta + 1) * sizeof(float4)));
+    CK(s.C.alloc(J.nc * sizeof(float)));
+    double* base = d_scr.as<double>() + scratch_off[i];
+    J.d = base;
+    J.ab = base + 2 * (size_t)(J.nmax + 1);
+    J.terms = J.ab + 4 * (size_t)(J.nstop + 1);
+    J.out = d_res.as<double>() + nres * i;
+    J.F = s.F.as<float4>();
+    J.S = s.S.as<float4>();
+    J.C = s.C.as<float>();
+  }
+  CK(d_jobs.alloc(n * sizeof(MieJob)));
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(d_jobs.p, jobs.data(), n * sizeof(MieJob), cudaMemcpyHostToDevice, st));
+  CK(launch_mie_tables(d_jobs.as<const MieJob>(), n, st));
+  std::vector<double> h(nres * n);
+  CK(cudaMemcpyAsync(h.data(), d_res.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int i = 0; i < n; ++i) {
+    const double* R = h.data() + nres * i;
+    if (!(R[0] >= 0) || !(R[1] > 0) || !std::isfinite(R[1]))
+      return set_err(MCRT_ENONCONV, "mcrt_mie_scatterers_create: the Mie series gave no finite omega and kl");
+    made[i]->omega = R[0];
+    made[i]->kl = R[1];
+  }
+  if (tables) std::memcpy(tables, h.data(), h.size() * sizeof(double));
+  for (int i = 0; i < n; ++i) out[i] = made[i].release();
   return MCRT_OK;
 }
 

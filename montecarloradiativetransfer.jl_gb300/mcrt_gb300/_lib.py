@@ -124,6 +124,8 @@ SIGNATURES = {
     "mcrt_batch_read": [_VP, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(Stats)],
     "mcrt_batch_timing": [_VP, _dp, _dp],
     "mcrt_batch_destroy": [_VP],
+    "mcrt_scatterer_params": [_VP, _dp, _dp],
+    "mcrt_mie_scatterers_create": [_VP, C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int, C.POINTER(_VP), _dp],
     "mcrt_run_rt": [_VP, C.POINTER(ConfigC), C.POINTER(GeometryC), C.POINTER(RunOpts), _dp, _dp, _dp,
                     C.POINTER(Stats)],
     "mcrt_measure_fp32_peak": [_VP, _dp],

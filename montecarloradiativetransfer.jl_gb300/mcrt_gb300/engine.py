@@ -28,8 +28,13 @@ class Context:
         self.h = h
         self.device = device
         self._scat: Dict[int, Tuple[object, C.c_void_p]] = {}
+        self._owned: List[C.c_void_p] = []
 
     def scatterer(self, s) -> C.c_void_p:
+        if isinstance(s, DeviceMieScatterer):
+            if s.ctx is not self:
+                raise ValueError("this scatterer's tables live on another context's device")
+            return s.handle
         key = id(s)
         hit = self._scat.get(key)
         if hit is not None and hit[0] is s:
@@ -66,6 +71,30 @@ class Context:
             gc = _lib.GeometryC(_lib.SPHERE, math.pi, 0.0, 1, layers)
         return gc, [layers]
 
+    def mie_scatterers(self, params: Sequence[Tuple[float, complex, float, float]], *, Ntheta: int = 181,
+                       random_points: int = 1000, with_tables: bool = False) -> List["DeviceMieScatterer"]:
+        """MieScatterer(r, m, λ, ν; Nθ, random_points) for each (r, m, λ, ν) in ``params``,
+        with bhmie and calculate_csrn run on the device in one launch
+        (mcrt_mie_scatterers_create); the tables stay in device memory. With
+        ``with_tables`` the FP64 tables are also copied back onto the returned objects."""
+        n = len(params)
+        r, mre, mim, lam, nu = (np.ascontiguousarray([f(p) for p in params], float) for f in (
+            lambda p: p[0], lambda p: complex(p[1]).real, lambda p: complex(p[1]).imag, lambda p: p[2],
+            lambda p: p[3]))
+        nres = 7 + 8 * Ntheta + random_points + 1
+        tab = np.zeros(n * nres) if with_tables else None
+        hs = (C.c_void_p * n)()
+        check(lib().mcrt_mie_scatterers_create(self.h, n, dptr(r), dptr(mre), dptr(mim), dptr(lam), dptr(nu),
+                                               int(Ntheta), int(random_points), hs,
+                                               dptr(tab) if tab is not None else None))
+        out = []
+        for i in range(n):
+            h = C.c_void_p(hs[i])
+            self._owned.append(h)
+            out.append(DeviceMieScatterer(self, h, params[i], Ntheta, random_points,
+                                          tab[i * nres:(i + 1) * nres] if tab is not None else None))
+        return out
+
     def fp32_peak_tflops(self) -> float:
         v = np.zeros(1)
         check(lib().mcrt_measure_fp32_peak(self.h, dptr(v)))
@@ -77,6 +106,9 @@ class Context:
             for _, h in self._scat.values():
                 L.mcrt_scatterer_destroy(h)
             self._scat.clear()
+            for h in self._owned:
+                L.mcrt_scatterer_destroy(h)
+            self._owned.clear()
             L.mcrt_ctx_destroy(self.h)
             self.h = None
 
@@ -85,6 +117,37 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+class DeviceMieScatterer:
+    """A MieScatterer whose tables were produced on, and stay on, one context's device
+    (Context.mie_scatterers). It stands wherever a MieScatterer does in a Layer or a
+    SphereGeometry run on that context."""
+
+    kind = _lib.MIE
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p, param, Ntheta: int, random_points: int, tables=None):
+        self.ctx, self.handle = ctx, handle
+        self.r, self.m, self.lam, self.nu = float(param[0]), complex(param[1]), float(param[2]), float(param[3])
+        self.x = 2 * math.pi * self.r / self.lam
+        self.Ntheta, self.random_points = int(Ntheta), int(random_points)
+        om, kl = C.c_double(), C.c_double()
+        check(lib().mcrt_scatterer_params(handle, C.byref(om), C.byref(kl)))
+        self.omega, self.kl = om.value, kl.value
+        if tables is not None:
+            n, rp = self.Ntheta, self.random_points
+            self.q_ext, self.q_sca, self.q_abs, self.q_back, self.asymm = (float(v) for v in tables[2:7])
+            o = 7
+            self.F11, self.F12, self.F33, self.F34 = (tables[o + k * n:o + (k + 1) * n].copy() for k in range(4))
+            o += 4 * n
+            self.S11 = tables[o:o + 2 * n:2] + 1j * tables[o + 1:o + 2 * n:2]
+            o += 2 * n
+            self.S22 = tables[o:o + 2 * n:2] + 1j * tables[o + 1:o + 2 * n:2]
+            o += 2 * n
+            self.csrn = tables[o:o + rp + 1].copy()
+
+    def __repr__(self) -> str:
+        return f"DeviceMieScatterer(x={self.x:.6g}, m={self.m}, omega={self.omega:.6g}, kl={self.kl:.6g})"
 
 
 _default: Optional[Context] = None
