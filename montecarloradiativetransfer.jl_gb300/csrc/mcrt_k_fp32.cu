@@ -3,7 +3,9 @@
 
 namespace mcrt {
 
-// Bins per lane: 4 RT polar angles, 2 CB bins; at most 128 registers per thread.
+// Bins per lane: 4 RT polar angles (8 for the 256-thread shape, which amortises the
+// per-event setup over more bins and measured 2% faster), 2 CB bins; at most 128
+// registers per thread.
 bool kernel_info_fp32(int bs, KInfo& k) {
   k.state_bytes = sizeof(PState<float>);
   switch (bs) {
@@ -12,7 +14,7 @@ bool kernel_info_fp32(int bs, KInfo& k) {
       k.shared_static = sizeof(Shared<float, 128>);
       return true;
     case 256:
-      k.fn = k_transport<float, 256, 4, 2, 2>;
+      k.fn = k_transport<float, 256, 8, 2, 2>;
       k.shared_static = sizeof(Shared<float, 256>);
       return true;
     case 512:
