@@ -879,8 +879,8 @@ int read_instance(Group& G, int user_index, double A_out[5], double* Irt, double
 
 // The autotuner: times the candidate launch shapes (threads per block, blocks per SM)
 // and, for Mie scatterers, the table staging (shared memory or global memory through
-// L1) on a sample of the workload's own photons, two per thread, and keeps the fastest
-// for this workload signature in the context. User-given fields are kept fixed.
+// L1) on the same sample of the workload's own photons, and keeps the fastest for this
+// workload signature in the context. User-given fields are kept fixed.
 int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const double* I0, uint64_t seed,
              uint32_t inst, long long nph, long long photon_begin, int rng_mode, const mcrt_run_opts* o,
              const std::string& sig) {
@@ -902,31 +902,37 @@ int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const 
   ctx_t::Tuned best{0, 0, 0, -1.0};
   std::vector<std::string> seen;
   bool warmed = false;
-  for (auto sh : shapes) {
-    for (int st : stagings) {
-      mcrt_run_opts oo{};
-      if (o) oo = *o;
-      oo.kernel = MCRT_KERNEL_PERSISTENT;
-      oo.block_size = sh.first;
-      oo.blocks_per_sm = sh.second;
-      oo.table_staging = st;
-      const long long ns = std::max<long long>(1, std::min<long long>(nph, 2LL * ctx->sms * sh.first *
-                                                                          std::max(sh.second, 1)));
-      Group T;
-      const mcrt_geometry* gs[1] = {g};
-      long long n1 = ns;
-      if (build_group(ctx, c, gs, I, &seed, &inst, &n1, photon_begin, rng_mode, 1, &oo, T)) continue;
-      std::string key = std::to_string(T.L.bs) + "x" + std::to_string(T.L.bpsm) + "/" + std::to_string(T.L.table_f4);
-      if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;  // occupancy folded it
-      seen.push_back(key);
-      for (int rep = warmed ? 1 : 0; rep < 2; ++rep) {  // the first launch also warms up the device
-        if (launch_group(T) || finish_group(T)) return MCRT_ECUDA;
-      }
-      warmed = true;
-      const double rate = ns / std::max(T.last_ms, 1e-3f);
-      if (rate > best.paths_per_ms) best = ctx_t::Tuned{T.L.bs, T.L.bpsm, st, rate};
+  // Every candidate runs the same photons (up to 4 per thread of the largest shape), so
+  // the rates compare steady-state throughput rather than the end-of-launch tail.
+  const long long ns = std::max<long long>(1, std::min<long long>(nph, 4LL * ctx->sms * 768));
+  auto trial = [&](std::pair<int, int> sh, int st) -> int {
+    mcrt_run_opts oo{};
+    if (o) oo = *o;
+    oo.kernel = MCRT_KERNEL_PERSISTENT;
+    oo.block_size = sh.first;
+    oo.blocks_per_sm = sh.second;
+    oo.table_staging = st;
+    Group T;
+    const mcrt_geometry* gs[1] = {g};
+    long long n1 = ns;
+    if (build_group(ctx, c, gs, I, &seed, &inst, &n1, photon_begin, rng_mode, 1, &oo, T)) return MCRT_OK;
+    std::string key = std::to_string(T.L.bs) + "x" + std::to_string(T.L.bpsm) + "/" + std::to_string(T.L.table_f4);
+    if (std::find(seen.begin(), seen.end(), key) != seen.end()) return MCRT_OK;  // occupancy folded it
+    seen.push_back(key);
+    for (int rep = warmed ? 1 : 0; rep < 2; ++rep) {  // the first launch also warms up the device
+      if (launch_group(T) || finish_group(T)) return MCRT_ECUDA;
     }
-  }
+    warmed = true;
+    const double rate = ns / std::max(T.last_ms, 1e-3f);
+    if (rate > best.paths_per_ms) best = ctx_t::Tuned{T.L.bs, T.L.bpsm, st, rate};
+    return MCRT_OK;
+  };
+  // launch shapes with the first staging choice, then the other stagings on the best shape
+  for (auto sh : shapes)
+    if (trial(sh, stagings[0])) return MCRT_ECUDA;
+  const std::pair<int, int> best_shape{best.bs, best.bpsm};
+  for (size_t k = 1; k < stagings.size(); ++k)
+    if (best.bs && trial(best_shape, stagings[k])) return MCRT_ECUDA;
   if (best.bs == 0) return set_err(MCRT_EINVAL, "autotune: no launch shape fits this workload");
   std::lock_guard<std::mutex> lk(ctx->mu);
   ctx->tuned[sig] = best;

@@ -1563,12 +1563,14 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
       const int tdn = !nd ? 0
                       : fr ? (B.lo1 - B.lo0 + 31) / 32
                            : (B.nphi * ((B.lo1 - B.lo0 + NBR - 1) / NBR) + 31) / 32;
-      // Work items are (tile, chunk of up to EVC events); the costlier CB items go first.
-      // Chunks only split batches larger than 256 events: below that, the extra tally
-      // flushes cost more than the better balance gains. Fourier RT tiles are few (one
-      // lane per polar bin) and flush 20 values per lane, so they take smaller chunks.
-      constexpr int EVC = 256, EVF = 64;
-      const int evr = fr ? EVF : EVC;
+      // Work items are (tile, chunk of events); the costlier CB items go first. CB chunks
+      // hold up to 256 events. RT chunks hold 128 events in blocks of up to 256 threads,
+      // which balances the end of the phase better (measured 5% faster on the Mie slab;
+      // 64 or 96 lose more to tally flushes than they gain), and 256 in larger blocks.
+      // Fourier RT tiles are few (one lane per polar bin) and flush 20 values per lane,
+      // so they take 64.
+      constexpr int EVC = 256, EVR = BS <= 256 ? 128 : 256, EVF = 64;
+      const int evr = fr ? EVF : EVR;
       const int ccb = (nc + EVC - 1) / EVC, cup = (nu + evr - 1) / evr, cdn = (nd + evr - 1) / evr;
       const int icb = tcb * ccb, iup = tup * cup, idn = tdn * cdn;
       const int total = icb + iup + idn;
@@ -1591,18 +1593,18 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
           if (fr)
             rt_fourier_tile<T, BS>(sh, B, w / cup, true, c * evr, min((c + 1) * evr, nu));
           else if constexpr (std::is_same<T, float>::value)
-            rt_tile_f2<NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
+            rt_tile_f2<NBR, BS>(sh, B, w / cup, true, pc, c * evr, min((c + 1) * evr, nu));
           else
-            rt_tile<T, NBR, BS>(sh, B, w / cup, true, pc, c * EVC, min((c + 1) * EVC, nu));
+            rt_tile<T, NBR, BS>(sh, B, w / cup, true, pc, c * evr, min((c + 1) * evr, nu));
         } else {
           w -= icb + iup;
           const int c = w % cdn;
           if (fr)
             rt_fourier_tile<T, BS>(sh, B, w / cdn, false, c * evr, min((c + 1) * evr, nd));
           else if constexpr (std::is_same<T, float>::value)
-            rt_tile_f2<NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
+            rt_tile_f2<NBR, BS>(sh, B, w / cdn, false, pc, c * evr, min((c + 1) * evr, nd));
           else
-            rt_tile<T, NBR, BS>(sh, B, w / cdn, false, pc, c * EVC, min((c + 1) * EVC, nd));
+            rt_tile<T, NBR, BS>(sh, B, w / cdn, false, pc, c * evr, min((c + 1) * evr, nd));
         }
       }
     }
