@@ -42,9 +42,12 @@ TOTAL_PHOTONS = 100_000_000
 FLOPS_RT_MIE = 128.349
 FLOPS_CBN_MIE = 409.0
 FLOPS_CB1_MIE = 196.0
-# DRAM bytes per launch of the transport kernel from ncu (scaled per photon from a
-# small capture); None until a capture has been summarised.
-NCU_DRAM_BYTES_PER_PHOTON = None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one transport launch
+# per photon, from an ncu capture of `bench.py --case 524288` (36.8 MB read + 6.07 GB
+# written for 524 288 photons). The traffic is
+# the per-event photon-state pool and scales with the photons, so a full launch is this
+# times its photons.
+NCU_DRAM_BYTES_PER_PHOTON = 11638.0
 
 
 def parse():
