@@ -205,6 +205,43 @@ def batch_leg(M, ctx, n_inst=256, scale=1e-3, seed=4):
             "paths_per_s": photons / (ms / 1e3)}
 
 
+def _scaled_err(a, b):
+    """max |a - b| over the largest |I| of b (Stokes tallies of shape (4, ...))."""
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    scale = np.max(np.abs(b[0])) if b.ndim >= 2 and b.shape[0] == 4 else np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / scale) if scale > 0 else float(np.max(np.abs(a)))
+
+
+def other_workloads_leg(M, ctx, n32=1 << 16, n64=1 << 12):
+    """The Rayleigh slab (Nθ = 180, 200 CB angles over 0-2°, τ = 10, ω = 0.99, normal
+    incidence) and the Mie sphere (τ = 20, x = 2, m = 1.31, 500 CB angles over 0-5°) at
+    bounded sizes: FP32 paths/s, FP64 paths/s, and the FP32-vs-FP64 scaled error of
+    every tally on identical Philox streams."""
+    I0 = [1.0, 0.0, 0.0, 0.0]
+    ray = M.RayleighScatterer(0.99, 100.0)
+    g1 = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=10 * ray.kl, scatterer=ray)])
+    tb1 = [math.radians(2.0) * i / 199 for i in range(200)]
+    mie2 = M.MieScatterer(2.0 / (2 * math.pi), 1.31 + 0j, 1.0, 0.1, Ntheta=1801)
+    g3 = M.SphereGeometry(R=20 * mie2.kl, scatterer=mie2)
+    tb3 = [math.radians(5.0) * i / 499 for i in range(500)]
+    runs = (("rayleigh_slab_tau10", g1, lambda n: M.Config(g1, number_of_rays=n, Ntheta=180, thetab=tb1,
+                                                             maximum_scattering_times=1000), 1),
+            ("mie_sphere_tau20", g3, lambda n: M.Config(g3, number_of_rays=n, thetab=tb3), 3))
+    out = {}
+    for name, g, mk, seed in runs:
+        r32 = M.simulate(mk(n32), g, I0, ctx=ctx, precision="fp32", seed=seed, with_extras=True)
+        a = M.simulate(mk(n64), g, I0, ctx=ctx, precision="fp32", seed=seed + 100, with_extras=True)
+        b = M.simulate(mk(n64), g, I0, ctx=ctx, precision="fp64", seed=seed + 100, with_extras=True)
+        out[name] = {
+            "fp32_paths_per_s": n32 / (r32[7]["stats"]["kernel_ms"] / 1e3), "fp32_photons": n32,
+            "fp64_paths_per_s": n64 / (b[7]["stats"]["kernel_ms"] / 1e3), "fp64_photons": n64,
+            "events_per_path": r32[7]["stats"]["events"] / n32,
+            "fp32_vs_fp64_scaled_err": {"A": _scaled_err(a[:5], b[:5]), "Irt": _scaled_err(a[5], b[5]),
+                                        "Icb": _scaled_err(a[6], b[6])},
+        }
+    return out
+
+
 def cpu_oracle_rate(M, n_sample, threads=0):
     """Times the oracle (the FP64 C++ restatement of the reference's CPU path) on a bounded
     sample of the same workload with all host threads."""
@@ -374,6 +411,12 @@ def main():
         s64.launch(0, np64)
         r64 = s64.read()
         s64.close()
+        # the FP32 kernel on the same photons and Philox streams: its error against FP64
+        s32 = M.Solve(cfg64.replace(number_of_rays=np64), g64, I0, ctx=ctx, precision="fp32", seed=2)
+        s32.launch(0, np64)
+        r32 = s32.read()
+        s32.close()
+        err32 = {k: _scaled_err(r32[k], r64[k]) for k in ("A", "Irt", "Icb", "ladder")}
         plain_threads = min(n64, 65536)
         sp = M.Solve(cfg64.replace(maximum_threads=plain_threads), g64, I0, ctx=ctx, precision="fp64",
                      kernel="plain", seed=2)
@@ -385,12 +428,15 @@ def main():
         cpu_v, cores, cpu_dt = cpu_oracle_rate(M, args.cpu_sample)
         serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
         batch = batch_leg(M, ctx)
+        others = other_workloads_leg(M, ctx)
         extras = {
+            "other_workloads": others,
             "serve": serve,
             "batch_uneven_slabs": batch,
             "fp64_persistent": {"value": v64, "unit": "paths/s", "sample_photons": np64},
             "fp64_plain": {"value": vplain, "unit": "paths/s", "sample_photons": n64,
                            "threads": plain_threads},
+            "fp32_vs_fp64_scaled_err": err32,
             "fp32_over_fp64_plain": value / world / vplain,
             "fp32_over_fp64_persistent": value / world / v64,
             "cpu_baseline": {"value": cpu_v, "unit": "paths/s", "cores": cores, "kind": "port",

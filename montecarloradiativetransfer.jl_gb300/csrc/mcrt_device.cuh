@@ -208,6 +208,15 @@ struct MT<float> {
   static __device__ __forceinline__ float floor(float x) { return floorf(x); }
   static __device__ __forceinline__ float fabs(float x) { return fabsf(x); }
   static __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
+  // Natural log of a positive FP32 norm, accumulated into an FP64 log scale: the MUFU
+  // log2 (relative error about 2^-22) instead of an FP64 log on the FP64 pipe.
+  static __device__ __forceinline__ double logscale(float x) { return (double)(__log2f(x) * 0.693147180559945309f); }
+  // exp of an FP64 log-scale difference, returned in FP32 (underflows to 0 as the cast would).
+  static __device__ __forceinline__ float expscale(double d) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)(d * 1.4426950408889634)));
+    return r;
+  }
   static constexpr float KEPLER_TOL = 4e-6f;
   static constexpr int KEPLER_CAP = 32;
 };
@@ -218,6 +227,8 @@ struct MT<double> {
   static __device__ __forceinline__ double exp2n(double x) { return ::exp2(-x); }
   static __device__ __forceinline__ double log(double x) { return ::log(x); }
   static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+  static __device__ __forceinline__ double logscale(double x) { return ::log(x); }
+  static __device__ __forceinline__ double expscale(double d) { return ::exp(d); }
   static __device__ __forceinline__ double acos(double x) { return ::acos(x); }
   static __device__ __forceinline__ double cbrt(double x) { return ::cbrt(x); }
   static __device__ __forceinline__ void sincos(double x, double* s, double* c) { ::sincos(x, s, c); }

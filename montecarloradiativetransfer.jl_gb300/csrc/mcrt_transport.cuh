@@ -274,7 +274,7 @@ __device__ bool start_photon(PState<T>& ps, const DevInstance& in, unsigned long
 template <typename T>
 __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTables<T>& B,
                             EventP<T>& ev, double* tacc, size_t stride, size_t g,
-                            unsigned* status, bool& dead) {
+                            unsigned* status, bool& dead, unsigned& attempts) {
   dead = false;
   const int n = ++ps.n;
   const DevScatterer& s1 = in.scat[in.layers[0].scat];
@@ -308,7 +308,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
       T na = MT<T>::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3]);
       T ina = T(1) / na;
       for (int s = 0; s < 4; ++s) ps.A[s] = a[s] * ina;
-      ps.logA += log((double)na);
+      ps.logA += MT<T>::logscale(na);
       if (n >= 3) {
         Frame<T> fm = spherical(-ps.k[0], -ps.k[1], -ps.k[2]);
         update_E_matrix(fm, -ps.kprev[0], -ps.kprev[1], -ps.kprev[2], s1.kind, s1.S, s1.ntheta, table_scale<T>(s1), m);
@@ -318,7 +318,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
         nl = MT<T>::sqrt(nl);
         T inl = T(1) / nl;
         for (int s = 0; s < 8; ++s) ps.L[s] *= inl;
-        ps.logL += log((double)nl);
+        ps.logL += MT<T>::logscale(nl);
       }
     }
     ps.kprev[0] = ps.k[0];
@@ -475,7 +475,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
     update_E(ks, Ef, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.S, s1.ntheta, table_scale<T>(s1));
     T nf = Ef[0] * Ef[0] + Ef[1] * Ef[1] + Ef[2] * Ef[2] + Ef[3] * Ef[3];
     T c = MT<T>::sqrt(Iaf0[0] / nf);
-    T rb = (T)exp(ps.logL - ps.logA) * c;
+    T rb = (T)MT<T>::expscale(ps.logL - ps.logA) * c;
     for (int s = 0; s < 4; ++s) {
       ev.ea[s] = ps.A[s] * c;
       ev.eb[s] = b[s] * rb;
@@ -503,12 +503,9 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
     }
   }
 
-  // Counters and the pending state change (applied now; the weight waits).
-  double evals_rt = (double)B.nphi * ((up ? (B.up1 - B.up0) : 0) + (dn ? (B.lo1 - B.lo0) : 0));
-  acc_add(tacc, stride, g, ACC_EVENTS, 1.0);
-  acc_add(tacc, stride, g, ACC_ATTEMPTS, (double)(a + 1));
-  acc_add(tacc, stride, g, ACC_RT, evals_rt);
-  if (cb) acc_add(tacc, stride, g, n > 1 ? ACC_CBN : ACC_CB1, (double)B.nthetab * B.nphib);
+  // The pending state change (applied now; the weight waits). The event counters are
+  // kept by the caller from the returned flags and attempts.
+  attempts = a + 1;
 
   T inv = T(1) / Ip[0];
   ps.Ih[0] = T(1);
@@ -1454,6 +1451,9 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
   bool alive = false;
   int pc = 0;
   PState<T> ps;
+  // per-thread event counters of the current instance (flushed when the block leaves it)
+  unsigned c_ev = 0, c_up = 0, c_dn = 0, c_cb1 = 0, c_cbn = 0;
+  unsigned long long c_att = 0;
   for (;;) {
     const DevInstance& in = sh.inst;
     const BinTables<T>& B = *reinterpret_cast<const BinTables<T>*>(in.bins);
@@ -1486,10 +1486,18 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
     int flags = 0;
     if (alive) {
       bool dead = false;
-      flags = sample_event<T>(ps, in, B, sh.ev[tid], p.tacc, stride, g, p.status, dead);
+      unsigned att = 0;
+      flags = sample_event<T>(ps, in, B, sh.ev[tid], p.tacc, stride, g, p.status, dead, att);
       if (dead) {
         alive = false;
         flags = 0;
+      } else {
+        ++c_ev;
+        c_att += att;
+        c_up += (flags & EV_UP) != 0;
+        c_dn += (flags & EV_DN) != 0;
+        c_cbn += (flags & EV_CBN) != 0;
+        c_cb1 += (flags & EV_CB) != 0 && (flags & EV_CBN) == 0;
       }
       sh.esc_up[tid] = T(0);
       sh.esc_dn[tid] = T(0);
@@ -1514,7 +1522,16 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
     if (nalive == 0) {
       if (!sh.exhausted) continue;
       // This block has finished its part of the instance: fold the per-thread
-      // accumulators into the instance's totals and move on.
+      // accumulators into the instance's totals and move on. The event counters were
+      // kept in registers (bin evaluations follow from the events' up/down/CB flags).
+      acc_add(p.tacc, stride, g, ACC_EVENTS, (double)c_ev);
+      acc_add(p.tacc, stride, g, ACC_ATTEMPTS, (double)c_att);
+      acc_add(p.tacc, stride, g, ACC_RT,
+              (double)B.nphi * ((double)c_up * (B.up1 - B.up0) + (double)c_dn * (B.lo1 - B.lo0)));
+      acc_add(p.tacc, stride, g, ACC_CB1, (double)c_cb1 * B.nthetab * B.nphib);
+      acc_add(p.tacc, stride, g, ACC_CBN, (double)c_cbn * B.nthetab * B.nphib);
+      c_ev = c_up = c_dn = c_cb1 = c_cbn = 0;
+      c_att = 0;
       for (int k = 0; k < NACC; ++k) {
         double v = p.tacc[(size_t)k * stride + g];
         p.tacc[(size_t)k * stride + g] = 0.0;
