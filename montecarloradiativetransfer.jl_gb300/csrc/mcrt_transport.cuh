@@ -1090,65 +1090,72 @@ struct CBLaneF2 {
   P2 lad;
 };
 
-// The reciprocal-path CB bins of src/gpu.jl:90-140 for one event, two bins per lane.
-template <bool MIE, bool SPHERE>
-__device__ __forceinline__ float cbn_event_f2(CBLaneF2& C, const EventP<float>& E, const DevScatterer& s1,
+// The reciprocal-path CB bins of src/gpu.jl:90-140 for one event, NPC pairs of bins per
+// lane; the event's frames and fields are set up once for all of the lane's pairs.
+template <int NPC, bool MIE, bool SPHERE>
+__device__ __forceinline__ float cbn_event_f2(CBLaneF2 (&CL)[NPC], const EventP<float>& E, const DevScatterer& s1,
                                               float tau0l, bool peak_lane) {
   const F2Frame FA = frame2(E.fct, E.fst, E.fcp, E.fsp);
   const F2Frame FB = frame2(E.bct, E.bst, E.bcp, E.bsp);
   const float scale = table_scale<float>(s1);
   const P2 M1 = p2s(-1.0f);
-  P2 ea[4], eb[4];
-  update_E2<MIE>(FA, E.ea, C.kx, C.ky, C.kz, C.ehx, C.ehy, s1.S, s1.ntheta, scale, ea);
-  update_E2<MIE>(FB, E.eb, C.kx, C.ky, C.kz, C.ehx, C.ehy, s1.S, s1.ntheta, scale, eb);
-  // Phase kl (ki + kf).(xa - xb) in turns, cancellation-free in the backscatter frame.
-  const P2 turns = fma2(C.c1, p2s(E.v1), fma2(C.c2, p2s(E.v2), C.c3 * p2s(E.v3)));
-  float sn0, cs0, sn1, cs1;
-  MT<float>::sincos_turns(turns.v.x - rintf(turns.v.x), &sn0, &cs0);
-  MT<float>::sincos_turns(turns.v.y - rintf(turns.v.y), &sn1, &cs1);
-  const P2 sn = p2(sn0, sn1), cs = p2(cs0, cs1), nsn = p2(-sn0, -sn1);
-  P2 ta2, tb2;
-  if (SPHERE) {
-    const P2 kxa = fma2(C.kx, p2s(E.xax), fma2(C.ky, p2s(E.xay), C.kz * p2s(E.xaz)));
-    const P2 kxb = fma2(C.kx, p2s(E.xbx), fma2(C.ky, p2s(E.xby), C.kz * p2s(E.xbz)));
-    ta2 = p2(sphere_t(kxa.v.x, E.Da), sphere_t(kxa.v.y, E.Da)) * p2s((float)LOG2E_D);
-    tb2 = p2(sphere_t(kxb.v.x, E.Db), sphere_t(kxb.v.y, E.Db)) * p2s((float)LOG2E_D);
-  } else {
-    ta2 = p2(C.upb0 ? E.a_up : E.a_dn, C.upb1 ? E.a_up : E.a_dn) * C.g;
-    tb2 = p2(C.upb0 ? E.b_up : E.b_dn, C.upb1 ? E.b_up : E.b_dn) * C.g;
-  }
-  tb2 = tb2 + p2s(E.tab2);
-  const bool ma0 = ta2.v.x <= tau0l, ma1 = ta2.v.y <= tau0l;
-  const P2 na = p2(ma0 ? MT<float>::exp2n(0.5f * ta2.v.x) : 0.f, ma1 ? MT<float>::exp2n(0.5f * ta2.v.y) : 0.f);
-  const P2 nb = p2(fabsf(tb2.v.x) <= tau0l ? MT<float>::exp2n(0.5f * tb2.v.x) : 0.f,
-                   fabsf(tb2.v.y) <= tau0l ? MT<float>::exp2n(0.5f * tb2.v.y) : 0.f);
+  float peak = 0.f;
 #pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    ea[s] = ea[s] * na;
-    eb[s] = eb[s] * nb;
+  for (int pp = 0; pp < NPC; ++pp) {
+    CBLaneF2& C = CL[pp];
+    P2 ea[4], eb[4];
+    update_E2<MIE>(FA, E.ea, C.kx, C.ky, C.kz, C.ehx, C.ehy, s1.S, s1.ntheta, scale, ea);
+    update_E2<MIE>(FB, E.eb, C.kx, C.ky, C.kz, C.ehx, C.ehy, s1.S, s1.ntheta, scale, eb);
+    // Phase kl (ki + kf).(xa - xb) in turns, cancellation-free in the backscatter frame.
+    const P2 turns = fma2(C.c1, p2s(E.v1), fma2(C.c2, p2s(E.v2), C.c3 * p2s(E.v3)));
+    float sn0, cs0, sn1, cs1;
+    MT<float>::sincos_turns(turns.v.x - rintf(turns.v.x), &sn0, &cs0);
+    MT<float>::sincos_turns(turns.v.y - rintf(turns.v.y), &sn1, &cs1);
+    const P2 sn = p2(sn0, sn1), cs = p2(cs0, cs1), nsn = p2(-sn0, -sn1);
+    P2 ta2, tb2;
+    if (SPHERE) {
+      const P2 kxa = fma2(C.kx, p2s(E.xax), fma2(C.ky, p2s(E.xay), C.kz * p2s(E.xaz)));
+      const P2 kxb = fma2(C.kx, p2s(E.xbx), fma2(C.ky, p2s(E.xby), C.kz * p2s(E.xbz)));
+      ta2 = p2(sphere_t(kxa.v.x, E.Da), sphere_t(kxa.v.y, E.Da)) * p2s((float)LOG2E_D);
+      tb2 = p2(sphere_t(kxb.v.x, E.Db), sphere_t(kxb.v.y, E.Db)) * p2s((float)LOG2E_D);
+    } else {
+      ta2 = p2(C.upb0 ? E.a_up : E.a_dn, C.upb1 ? E.a_up : E.a_dn) * C.g;
+      tb2 = p2(C.upb0 ? E.b_up : E.b_dn, C.upb1 ? E.b_up : E.b_dn) * C.g;
+    }
+    tb2 = tb2 + p2s(E.tab2);
+    const bool ma0 = ta2.v.x <= tau0l, ma1 = ta2.v.y <= tau0l;
+    const P2 na = p2(ma0 ? MT<float>::exp2n(0.5f * ta2.v.x) : 0.f, ma1 ? MT<float>::exp2n(0.5f * ta2.v.y) : 0.f);
+    const P2 nb = p2(fabsf(tb2.v.x) <= tau0l ? MT<float>::exp2n(0.5f * tb2.v.x) : 0.f,
+                     fabsf(tb2.v.y) <= tau0l ? MT<float>::exp2n(0.5f * tb2.v.y) : 0.f);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      ea[s] = ea[s] * na;
+      eb[s] = eb[s] * nb;
+    }
+    const P2 Ia = fma2(ea[0], ea[0], fma2(ea[1], ea[1], fma2(ea[2], ea[2], ea[3] * ea[3])));
+    const P2 Ib = fma2(eb[0], eb[0], fma2(eb[1], eb[1], fma2(eb[2], eb[2], eb[3] * eb[3])));
+    const P2 c1r = fma2(ea[0], cs, fma2(ea[1], nsn, eb[0])), c1i = fma2(ea[0], sn, fma2(ea[1], cs, eb[1]));
+    const P2 c2r = fma2(ea[2], cs, fma2(ea[3], nsn, eb[2])), c2i = fma2(ea[2], sn, fma2(ea[3], cs, eb[3]));
+    const P2 qh = fma2(c1r, c1r, c1i * c1i), qv = fma2(c2r, c2r, c2i * c2i);
+    P2 S0 = qh + qv, S1 = fma2(qh, M1, qv);
+    P2 S2 = fma2(c2r, c1r, c2i * c1i) * p2s(2.0f);
+    P2 S3 = fma2(c2i, c1r, (c2r * c1i) * M1) * p2s(-2.0f);
+    const P2 den = Ia + Ib;
+    const P2 scl = p2(den.v.x > 0.f ? __fdividef(Ia.v.x, den.v.x) : 0.f,
+                      den.v.y > 0.f ? __fdividef(Ia.v.y, den.v.y) : 0.f);
+    S0 = S0 * scl;
+    S1 = S1 * scl;
+    S2 = S2 * scl;
+    S3 = S3 * scl;
+    const P2 R1 = fma2(C.cf, S1, C.sf * S2), R2 = fma2(C.cf, S2, (C.sf * S1) * M1);
+    C.acc[0] = C.acc[0] + S0;
+    C.acc[1] = C.acc[1] + R1;
+    C.acc[2] = C.acc[2] + R2;
+    C.acc[3] = C.acc[3] + S3;
+    C.lad = C.lad + Ia;
+    if (pp == 0) peak = S0.v.x;  // bin 0 of the grid is the x half of a lane's first pair
   }
-  const P2 Ia = fma2(ea[0], ea[0], fma2(ea[1], ea[1], fma2(ea[2], ea[2], ea[3] * ea[3])));
-  const P2 Ib = fma2(eb[0], eb[0], fma2(eb[1], eb[1], fma2(eb[2], eb[2], eb[3] * eb[3])));
-  const P2 c1r = fma2(ea[0], cs, fma2(ea[1], nsn, eb[0])), c1i = fma2(ea[0], sn, fma2(ea[1], cs, eb[1]));
-  const P2 c2r = fma2(ea[2], cs, fma2(ea[3], nsn, eb[2])), c2i = fma2(ea[2], sn, fma2(ea[3], cs, eb[3]));
-  const P2 qh = fma2(c1r, c1r, c1i * c1i), qv = fma2(c2r, c2r, c2i * c2i);
-  P2 S0 = qh + qv, S1 = fma2(qh, M1, qv);
-  P2 S2 = fma2(c2r, c1r, c2i * c1i) * p2s(2.0f);
-  P2 S3 = fma2(c2i, c1r, (c2r * c1i) * M1) * p2s(-2.0f);
-  const P2 den = Ia + Ib;
-  const P2 scl = p2(den.v.x > 0.f ? __fdividef(Ia.v.x, den.v.x) : 0.f,
-                    den.v.y > 0.f ? __fdividef(Ia.v.y, den.v.y) : 0.f);
-  S0 = S0 * scl;
-  S1 = S1 * scl;
-  S2 = S2 * scl;
-  S3 = S3 * scl;
-  const P2 R1 = fma2(C.cf, S1, C.sf * S2), R2 = fma2(C.cf, S2, (C.sf * S1) * M1);
-  C.acc[0] = C.acc[0] + S0;
-  C.acc[1] = C.acc[1] + R1;
-  C.acc[2] = C.acc[2] + R2;
-  C.acc[3] = C.acc[3] + S3;
-  C.lad = C.lad + Ia;
-  return peak_lane ? S0.v.x : 0.f;
+  return peak_lane ? peak : 0.f;
 }
 
 // ------------------------------------------------------------------ collect: CB tile
@@ -1326,9 +1333,9 @@ __device__ void cb_tile(Shared<T, BS>& sh, const BinTables<T>& B, int tile, int 
 }
 
 // ------------------------------------------------------------------ collect: CB tile, FP32x2 lanes
-template <int BS>
+template <int BS, int NPC>
 __device__ void cb_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int tile, int pc, int q0, int q1) {
-  constexpr int NB = 2;
+  constexpr int NB = 2 * NPC;
   const int lane = threadIdx.x & 31;
   const int ngrp = (B.nthetab + NB - 1) / NB;
   const int item = tile * 32 + lane;
@@ -1343,23 +1350,27 @@ __device__ void cb_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
     okb[i] = lane_ok && j1 < B.nthetab;
     bb[i] = okb[i] ? j2 * B.nthetab + j1 : 0;
   }
-  CBLaneF2 C;
-  C.kx = p2(B.kfx[bb[0]], B.kfx[bb[1]]);
-  C.ky = p2(B.kfy[bb[0]], B.kfy[bb[1]]);
-  C.kz = p2(B.kfz[bb[0]], B.kfz[bb[1]]);
-  C.ehx = p2(B.ehx[bb[0]], B.ehx[bb[1]]);
-  C.ehy = p2(B.ehy[bb[0]], B.ehy[bb[1]]);
-  C.g = p2(B.gb[bb[0]], B.gb[bb[1]]);
-  C.cf = p2(B.cf2[bb[0]], B.cf2[bb[1]]);
-  C.sf = p2(B.sf2[bb[0]], B.sf2[bb[1]]);
-  C.c1 = p2(B.c1[bb[0]], B.c1[bb[1]]);
-  C.c2 = p2(B.c2[bb[0]], B.c2[bb[1]]);
-  C.c3 = p2(B.c3[bb[0]], B.c3[bb[1]]);
-  C.upb0 = B.upb[bb[0]] != 0;
-  C.upb1 = B.upb[bb[1]] != 0;
+  CBLaneF2 C[NPC];
 #pragma unroll
-  for (int s = 0; s < 4; ++s) C.acc[s] = p2s(0.f);
-  C.lad = p2s(0.f);
+  for (int pp = 0; pp < NPC; ++pp) {
+    const int b0 = bb[2 * pp], b1 = bb[2 * pp + 1];
+    C[pp].kx = p2(B.kfx[b0], B.kfx[b1]);
+    C[pp].ky = p2(B.kfy[b0], B.kfy[b1]);
+    C[pp].kz = p2(B.kfz[b0], B.kfz[b1]);
+    C[pp].ehx = p2(B.ehx[b0], B.ehx[b1]);
+    C[pp].ehy = p2(B.ehy[b0], B.ehy[b1]);
+    C[pp].g = p2(B.gb[b0], B.gb[b1]);
+    C[pp].cf = p2(B.cf2[b0], B.cf2[b1]);
+    C[pp].sf = p2(B.sf2[b0], B.sf2[b1]);
+    C[pp].c1 = p2(B.c1[b0], B.c1[b1]);
+    C[pp].c2 = p2(B.c2[b0], B.c2[b1]);
+    C[pp].c3 = p2(B.c3[b0], B.c3[b1]);
+    C[pp].upb0 = B.upb[b0] != 0;
+    C[pp].upb1 = B.upb[b1] != 0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) C[pp].acc[s] = p2s(0.f);
+    C[pp].lad = p2s(0.f);
+  }
   const bool peak_lane = lane_ok && j2 == 0 && grp == 0;
   const DevInstance& in = sh.inst;
   const DevScatterer& s1 = in.scat[in.layers[0].scat];
@@ -1371,11 +1382,11 @@ __device__ void cb_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
     const EventP<float>& E = sh.ev[e];
     float pk;
     if (mie)
-      pk = sphere ? cbn_event_f2<true, true>(C, E, s1, tau0l, peak_lane)
-                  : cbn_event_f2<true, false>(C, E, s1, tau0l, peak_lane);
+      pk = sphere ? cbn_event_f2<NPC, true, true>(C, E, s1, tau0l, peak_lane)
+                  : cbn_event_f2<NPC, true, false>(C, E, s1, tau0l, peak_lane);
     else
-      pk = sphere ? cbn_event_f2<false, true>(C, E, s1, tau0l, peak_lane)
-                  : cbn_event_f2<false, false>(C, E, s1, tau0l, peak_lane);
+      pk = sphere ? cbn_event_f2<NPC, false, true>(C, E, s1, tau0l, peak_lane)
+                  : cbn_event_f2<NPC, false, false>(C, E, s1, tau0l, peak_lane);
     if (peak_lane) sh.peak[e] = pk;
   }
   // Order-1 events (a few per path) use the scalar single-scattering bins.
@@ -1410,8 +1421,11 @@ __device__ void cb_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
       if (peak_lane) sh.peak[e] = pk;
     }
 #pragma unroll
-    for (int s = 0; s < 4; ++s) C.acc[s] = C.acc[s] + p2(Cs.acc[0][s], Cs.acc[1][s]);
-    C.lad = C.lad + p2(Cs.lad[0], Cs.lad[1]);
+    for (int pp = 0; pp < NPC; ++pp) {
+#pragma unroll
+      for (int s = 0; s < 4; ++s) C[pp].acc[s] = C[pp].acc[s] + p2(Cs.acc[2 * pp][s], Cs.acc[2 * pp + 1][s]);
+      C[pp].lad = C[pp].lad + p2(Cs.lad[2 * pp], Cs.lad[2 * pp + 1]);
+    }
   }
   if (lane_ok) {
 #pragma unroll
@@ -1419,8 +1433,9 @@ __device__ void cb_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
       if (okb[i]) {
         double* dst = in.Icb + 4 * (size_t)bb[i];
 #pragma unroll
-        for (int s = 0; s < 4; ++s) atomicAdd(dst + s, (double)(i ? C.acc[s].v.y : C.acc[s].v.x));
-        atomicAdd(in.ladder + bb[i], (double)(i ? C.lad.v.y : C.lad.v.x));
+        for (int s = 0; s < 4; ++s)
+          atomicAdd(dst + s, (double)((i & 1) ? C[i / 2].acc[s].v.y : C[i / 2].acc[s].v.x));
+        atomicAdd(in.ladder + bb[i], (double)((i & 1) ? C[i / 2].lad.v.y : C[i / 2].lad.v.x));
       }
     }
   }
@@ -1600,8 +1615,8 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
         if (w >= total) break;
         if (w < icb) {
           const int c = w % ccb;
-          if constexpr (std::is_same<T, float>::value && NBC == 2)
-            cb_tile_f2<BS>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
+          if constexpr (std::is_same<T, float>::value && NBC % 2 == 0)
+            cb_tile_f2<BS, NBC / 2>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
           else
             cb_tile<T, NBC, BS>(sh, B, w / ccb, pc, c * EVC, min((c + 1) * EVC, nc));
         } else if (w < icb + iup) {

@@ -32,7 +32,7 @@ def small_cfg(M, g, n, **kw):
 
 def geometry(M, case, mie5, mie2):
     ray = M.RayleighScatterer(0.99, 100.0)
-    if case in ("plane_rayleigh", "plane_rayleigh_nphi4", "plane_rayleigh_full_bins"):
+    if case in ("plane_rayleigh", "plane_rayleigh_nphi4", "plane_rayleigh_full_bins", "plane_rayleigh_uneven_phi"):
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), N0
     if case == "plane_rayleigh_V":
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), [1, 0, 0, -1]
@@ -50,11 +50,13 @@ def geometry(M, case, mie5, mie2):
 
 
 CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite",
-         "plane_rayleigh_nphi4", "plane_rayleigh_full_bins"]
+         "plane_rayleigh_nphi4", "plane_rayleigh_full_bins", "plane_rayleigh_uneven_phi"]
 # Bin grids other than small_cfg's. A slab of Rayleigh scatterers tallies RT through
 # azimuthal Fourier modes when Nphi >= 5; Nphi = 4 keeps the per-bin evaluation, and the
 # full grid is the reference's default (64 x 48 RT bins).
-CASE_BINS = {"plane_rayleigh_nphi4": {"Nphi": 4}, "plane_rayleigh_full_bins": {"Ntheta": 64, "Nphi": 48}}
+CASE_BINS = {"plane_rayleigh_nphi4": {"Nphi": 4}, "plane_rayleigh_full_bins": {"Ntheta": 64, "Nphi": 48},
+             # an irregular azimuth grid: the Fourier tally is expanded at the given angles
+             "plane_rayleigh_uneven_phi": {"Nphi": 7, "phi": [0.0, 0.3, 1.1, 2.0, 3.5, 4.4, 6.0]}}
 
 
 @pytest.mark.parametrize("case", CASES)
