@@ -902,9 +902,28 @@ int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const 
   ctx_t::Tuned best{0, 0, 0, -1.0};
   std::vector<std::string> seen;
   bool warmed = false;
-  // Every candidate runs the same photons (up to 4 per thread of the largest shape), so
-  // the rates compare steady-state throughput rather than the end-of-launch tail.
-  const long long ns = std::max<long long>(1, std::min<long long>(nph, 4LL * ctx->sms * 768));
+  // Every candidate runs the same photons, so the rates compare steady-state throughput
+  // rather than the end-of-launch tail: up to 4 per thread of the largest shape, fewer
+  // when a probe launch (which also warms up the device) shows that a candidate would
+  // take more than about a second.
+  long long ns = std::max<long long>(1, std::min<long long>(nph, 4LL * ctx->sms * 768));
+  {
+    mcrt_run_opts oo{};
+    if (o) oo = *o;
+    oo.kernel = MCRT_KERNEL_PERSISTENT;
+    oo.block_size = shapes[0].first;
+    oo.blocks_per_sm = shapes[0].second;
+    oo.table_staging = stagings[0];
+    Group T;
+    const mcrt_geometry* gs[1] = {g};
+    long long n1 = std::min<long long>(ns, (long long)ctx->sms * 256);
+    if (!build_group(ctx, c, gs, I, &seed, &inst, &n1, photon_begin, rng_mode, 1, &oo, T)) {
+      if (launch_group(T) || finish_group(T)) return MCRT_ECUDA;
+      warmed = true;
+      const double per_ms = n1 / std::max(T.last_ms, 1e-3f);
+      ns = std::max<long long>(n1, std::min<long long>(ns, (long long)(per_ms * 1000.0)));
+    }
+  }
   auto trial = [&](std::pair<int, int> sh, int st) -> int {
     mcrt_run_opts oo{};
     if (o) oo = *o;

@@ -43,6 +43,10 @@ def geometry(M, case, mie5, mie2):
     if case == "two_layers":
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1 * ray.kl, scatterer=ray),
                                               M.Layer(d=2 * mie5.kl, scatterer=mie5)]), N0
+    if case == "two_layers_rayleigh":  # Fourier RT tally across layers of different albedo
+        ray2 = M.RayleighScatterer(0.9, 50.0)
+        return M.PlaneGeometry(math.radians(160), 0.7, [M.Layer(d=1 * ray.kl, scatterer=ray),
+                                                        M.Layer(d=2 * ray2.kl, scatterer=ray2)]), [1, 0, 1, 0]
     if case == "semi_infinite":
         return M.PlaneGeometry(math.radians(170), 0.0, [M.Layer(d=1 * ray.kl, scatterer=ray),
                                                         M.Layer(d=-1.0, scatterer=ray, tau=math.inf)]), [1, 1, 0, 0]
@@ -50,7 +54,7 @@ def geometry(M, case, mie5, mie2):
 
 
 CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite",
-         "plane_rayleigh_nphi4", "plane_rayleigh_full_bins", "plane_rayleigh_uneven_phi"]
+         "plane_rayleigh_nphi4", "plane_rayleigh_full_bins", "plane_rayleigh_uneven_phi", "two_layers_rayleigh"]
 # Bin grids other than small_cfg's. A slab of Rayleigh scatterers tallies RT through
 # azimuthal Fourier modes when Nphi >= 5; Nphi = 4 keeps the per-bin evaluation, and the
 # full grid is the reference's default (64 x 48 RT bins).
