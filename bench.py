@@ -259,7 +259,7 @@ def cpu_oracle_rate(M, n_sample, threads=0):
 
 def run_reference(args, rank):
     """The reference arm: the reference's CPU algorithm (as the FP64 C++ oracle port,
-    since Julia is not installed) on the machine's host cores, same workload and metric."""
+    since Julia is not installed) on the host's cores, same workload and metric."""
     if rank != 0:
         return
     import mcrt_gb300 as M
