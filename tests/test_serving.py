@@ -105,3 +105,24 @@ def test_graph_replay_matches_direct_launches(M, gpu_ctx, mie5, mie2):
         srv.close()
     for a, b in zip(*outs):
         compare(a[:3], b[:3], 1e-9)
+
+
+def test_requests_with_device_made_mie_tables(M, gpu_ctx):
+    """A serving stream whose requests bring new (x, m): the tables are made on the device
+    in one launch (mcrt_mie_scatterers_create) and the requests run on them; each result
+    equals simulate() with the same device-made scatterer."""
+    rng = np.random.default_rng(11)
+    params = [(float(x) / (2 * math.pi), complex(rng.uniform(1.3, 1.6), 10 ** rng.uniform(-5, -2)), 1.0, 0.1)
+              for x in rng.uniform(0.5, 10.0, 4)]
+    scats = gpu_ctx.mie_scatterers(params, Ntheta=721)
+    srv = M.Server(ctx=gpu_ctx, precision="fp64", wave_photons=2048, min_quantum=256)
+    reqs = []
+    for i, sc in enumerate(scats):
+        g = M.PlaneGeometry(math.radians(150 + 5 * i), 0.1 * i, [M.Layer(d=(0.5 + i) * sc.kl, scatterer=sc)])
+        reqs.append((small_cfg(M, g), g, 300 + 200 * i, 50 + i))
+    tickets = [srv.submit(c, g, N0, n, seed=s, instance=0) for c, g, n, s in reqs]
+    for t, (c, g, n, s) in zip(tickets, reqs):
+        A, Irt, Icb, lad, info = srv.result(t)
+        solo = M.simulate(c.replace(number_of_rays=n), g, N0, ctx=gpu_ctx, precision="fp64", seed=s, instance=0)
+        compare((A, Irt, Icb), (np.array(solo[:5]), solo[5], solo[6]), 1e-9)
+    srv.close()
