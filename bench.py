@@ -64,6 +64,9 @@ def parse():
                     help="run one FP32 launch of the workload with this many photons and exit "
                          "(the small case for ncu captures)")
     ap.add_argument("--case-precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--case-workload", default="mie_slab", choices=["mie_slab", "rayleigh_slab", "mie_sphere"],
+                    help="workload of --case: the Mie slab, the Rayleigh slab (tau 10, Ntheta 180, 200 "
+                         "CB angles) or the Mie sphere (tau 20, x 2, 500 CB angles)")
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--serve-scale", type=float, default=1e-3, help="photon budget multiplier of the stream")
     return ap.parse_args()
@@ -306,7 +309,17 @@ def main():
     import mcrt_gb300 as M
 
     if args.case > 0:
-        mie, g, cfg = workload(M, args.case)
+        if args.case_workload == "mie_slab":
+            mie, g, cfg = workload(M, args.case)
+        elif args.case_workload == "rayleigh_slab":
+            ray = M.RayleighScatterer(0.99, 100.0)
+            g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=10 * ray.kl, scatterer=ray)])
+            cfg = M.Config(g, number_of_rays=args.case, Ntheta=180, maximum_scattering_times=1000,
+                           thetab=[math.radians(2.0) * i / 199 for i in range(200)])
+        else:
+            mie2 = M.MieScatterer(2.0 / (2 * math.pi), 1.31 + 0j, 1.0, 0.1, Ntheta=1801)
+            g = M.SphereGeometry(R=20 * mie2.kl, scatterer=mie2)
+            cfg = M.Config(g, number_of_rays=args.case, thetab=[math.radians(5.0) * i / 499 for i in range(500)])
         out = M.simulate(cfg, g, [1.0, 0.0, 0.0, 0.0], precision=args.case_precision, seed=2,
                          block_size=256, blocks_per_sm=2 if args.case_precision == "fp32" else 1,
                          table_staging="shared", with_extras=True)
