@@ -68,7 +68,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(compile_one, units))
     tmp = LIB + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"])
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread", "-ldl"])
     os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB} in {time.time() - t0:.1f}s")

@@ -16,6 +16,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "mcrt.h"
 #include "mcrt_device.cuh"
 #include "mcrt_host.h"
@@ -23,6 +25,15 @@
 #include "mcrt_mie.cuh"
 
 using namespace mcrt;
+
+namespace {
+// NVTX range for the host-side phases (upload, launch, read-back, serving waves), so a
+// timeline profiler shows them beside the kernels. Costs nothing without a tool attached.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace {
 
@@ -303,6 +314,7 @@ int mcrt_mie_scatterers_create(mcrt_ctx* ctx, int n, const double* r, const doub
   }
   CK(d_jobs.alloc(n * sizeof(MieJob)));
   cudaStream_t st = ctx->stream;
+  Range rr("mcrt mie tables");
   CK(cudaMemcpyAsync(d_jobs.p, jobs.data(), n * sizeof(MieJob), cudaMemcpyHostToDevice, st));
   CK(launch_mie_tables(d_jobs.as<const MieJob>(), n, st));
   std::vector<double> h(nres * n);
@@ -712,6 +724,7 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
                 const double (*I0)[4], const uint64_t* seeds, const uint32_t* insts,
                 const long long* nph, long long photon_begin, int rng_mode, int n,
                 const mcrt_run_opts* o, Group& G) {
+  Range r("mcrt build group");
   G.ctx = ctx;
   G.n_inst = n;
   G.hinst.resize(n);
@@ -802,6 +815,7 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
 }
 
 int launch_group(Group& G) {
+  Range r("mcrt launch");
   mcrt_ctx* ctx = G.ctx;
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
@@ -847,6 +861,7 @@ int finish_group(Group& G) {
 
 int read_instance(Group& G, int user_index, double A_out[5], double* Irt, double* Icb, double* lad,
                   mcrt_stats* stats) {
+  Range r("mcrt read tallies");
   CK(cudaStreamSynchronize(G.ctx->stream));
   std::vector<double> h(G.per_inst);
   const double* src = G.hinst[user_index].Irt;
@@ -884,6 +899,7 @@ int read_instance(Group& G, int user_index, double A_out[5], double* Irt, double
 int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const double* I0, uint64_t seed,
              uint32_t inst, long long nph, long long photon_begin, int rng_mode, const mcrt_run_opts* o,
              const std::string& sig) {
+  Range r("mcrt autotune");
   const int prec = o ? o->precision : MCRT_FP32;
   std::vector<std::pair<int, int>> shapes;
   if (prec == MCRT_FP32)
@@ -1270,6 +1286,7 @@ int mcrt_run_rt(mcrt_ctx* ctx, const mcrt_config* cfg, const mcrt_geometry* g, c
   a.norm_cb = dn + a.nt;
   a.out_rt = dn + nrm.size();
   a.out_cb = a.out_rt + n_rt;
+  Range rr("mcrt run_rt epilogue");
   const int items = plane ? a.nt * a.np + a.ntb * a.npb : a.nt + a.ntb;
   if (plane)
     k_run_rt_plane<<<(items + 127) / 128, 128, 0, st>>>(a);
@@ -1525,6 +1542,7 @@ int srv_retire(mcrt_server* S, int b) {
 }
 
 int srv_launch(mcrt_server* S, int b) {
+  Range r("mcrt serve wave");
   auto& sl = S->slot[b];
   if (S->o.use_graphs) {
     CK(cudaEventRecord(sl.start, S->stream));
