@@ -129,6 +129,8 @@ typedef struct {
   int blocks_per_sm;    /* persistent: 0 = autotuned (or the most that fit) */
   int plain_threads;    /* plain: 0 = min(maximum_threads, number_of_rays) */
   int table_staging;    /* persistent: 0 = autotuned, 1 = shared memory, 2 = global memory (L1) */
+  int64_t max_attempts; /* cap of every rejection loop; 0 = 2^20. A loop that reaches it ends its
+                           photon and sets MCRT_FLAG_REJECT_LIMIT (the call returns MCRT_ENONCONV). */
 } mcrt_run_opts;
 
 /* Diagnostics returned beside the tallies (all raw sums over the photons run). */

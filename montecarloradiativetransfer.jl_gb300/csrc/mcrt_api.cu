@@ -546,6 +546,7 @@ int make_instance(const mcrt_config* c, const mcrt_geometry* g, const double I0[
                   uint32_t instance, int rng_mode, long long n_photons, long long photon_begin,
                   DevInstance& D, host::Sph& kfs_out) {
   std::memset(&D, 0, sizeof(D));
+  D.max_attempts = 1LL << 20;
   D.geom = g->kind;
   D.n_layers = g->n_layers;
   std::vector<const mcrt_scatterer*> sc;
@@ -733,6 +734,7 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
     int rc = make_instance(c, geoms[i], I0[i], seeds[i], insts[i], rng_mode, nph[i], photon_begin,
                            G.hinst[i], kfs[i]);
     if (rc) return rc;
+    if (o && o->max_attempts > 0) G.hinst[i].max_attempts = o->max_attempts;
   }
   // order instances by photon budget, largest first (blocks walk the list in order)
   G.order.resize(n);
@@ -1970,6 +1972,7 @@ extern "C" int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, cons
   rc = make_instance(cfg, g, I0, opts ? opts->seed : 0, opts ? opts->instance : 0, opts ? opts->rng_mode : 0,
                      cfg->number_of_rays, opts ? opts->photon_begin : 0, D, kfs);
   if (rc) return rc;
+  if (opts && opts->max_attempts > 0) D.max_attempts = opts->max_attempts;
   HostBins H = make_bins(cfg, g->kind, kfs);
 
   // Launch shape: one block per SM.

@@ -81,6 +81,7 @@ struct __align__(16) DevInstance {
   long long n_photons;     // photons of this instance in this launch
   long long photon_begin;  // first photon index (Philox counter)
   long long nrays;         // number_of_rays (stratified test mode)
+  long long max_attempts;  // cap of every rejection loop (a loop reaching it sets MCRT_FLAG_REJECT_LIMIT)
   unsigned key0, key1;
   int rng_mode;
   int rt_fourier;          // plane with Rayleigh scatterers only: RT bins by azimuthal Fourier modes

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) k_plain(PlainParams p) {
           } else {
             t = tp + T(1);
             for (unsigned a = 0; t > tp; ++a) {
-              if (a >= (1u << 20)) {
+              if ((long long)a >= in.max_attempts) {
                 atomicOr(p.status, 1u);
                 t = tp;
                 break;
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) k_plain(PlainParams p) {
         } else {
           t = tp + T(1);
           for (unsigned a = 0; t > tp; ++a) {
-            if (a >= (1u << 20)) {
+            if ((long long)a >= in.max_attempts) {
               atomicOr(p.status, 1u);
               t = tp;
               break;
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(256) k_plain(PlainParams p) {
       unsigned a = 0;
       int kcap = 0;
       for (;; ++a) {
-        if (a >= (1u << 20)) {
+        if ((long long)a >= in.max_attempts) {
           atomicOr(p.status, 1u);
           dead = true;
           break;

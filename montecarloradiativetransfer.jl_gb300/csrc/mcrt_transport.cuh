@@ -32,7 +32,6 @@
 namespace mcrt {
 
 constexpr int EV_UP = 1, EV_DN = 2, EV_CB = 4, EV_CBN = 8;
-constexpr unsigned MAX_ATTEMPTS = 1u << 20;
 
 template <typename T>
 struct __align__(16) EventP {
@@ -223,7 +222,7 @@ __device__ bool start_photon(PState<T>& ps, const DevInstance& in, unsigned long
       } else {
         t = tp + 1;
         for (unsigned a = 0; t > tp; ++a) {
-          if (a >= MAX_ATTEMPTS) {
+          if ((long long)a >= in.max_attempts) {
             atomicOr(status, 1u);
             acc_add(tacc, stride, g, ACC_REJECT_CAP, 1.0);
             t = tp;
@@ -241,7 +240,7 @@ __device__ bool start_photon(PState<T>& ps, const DevInstance& in, unsigned long
     } else {
       t = tp + 1;
       for (unsigned a = 0; t > tp; ++a) {
-        if (a >= MAX_ATTEMPTS) {
+        if ((long long)a >= in.max_attempts) {
           atomicOr(status, 1u);
           acc_add(tacc, stride, g, ACC_REJECT_CAP, 1.0);
           t = tp;
@@ -338,7 +337,7 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
   unsigned a = 0;
   int kcap = 0;
   for (;; ++a) {
-    if (a >= MAX_ATTEMPTS) {
+    if ((long long)a >= in.max_attempts) {
       atomicOr(status, 1u);
       acc_add(tacc, stride, g, ACC_REJECT_CAP, 1.0);
       dead = true;

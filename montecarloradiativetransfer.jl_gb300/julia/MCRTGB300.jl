@@ -80,10 +80,11 @@ struct RunOpts                  # mcrt_run_opts
     blocks_per_sm::Cint
     plain_threads::Cint
     table_staging::Cint
+    max_attempts::Int64         # 0 = the default rejection-loop cap
 end
 
 RunOpts(; precision = 0, kernel = 0, seed = rand(UInt64), instance = 0) =
-    RunOpts(precision, kernel, seed, instance, 0, 0, 0, 0, 0, 0)
+    RunOpts(precision, kernel, seed, instance, 0, 0, 0, 0, 0, 0, 0)
 
 # ---------------------------------------------------------------- context and errors
 const CTX = Ref{Ptr{Cvoid}}(C_NULL)

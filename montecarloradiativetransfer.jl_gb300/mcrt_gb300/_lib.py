@@ -59,7 +59,7 @@ class RunOpts(C.Structure):
         ("precision", C.c_int), ("kernel", C.c_int), ("seed", C.c_uint64),
         ("instance", C.c_uint32), ("rng_mode", C.c_int), ("photon_begin", C.c_int64),
         ("block_size", C.c_int), ("blocks_per_sm", C.c_int), ("plain_threads", C.c_int),
-        ("table_staging", C.c_int),
+        ("table_staging", C.c_int), ("max_attempts", C.c_int64),
     ]
 
 

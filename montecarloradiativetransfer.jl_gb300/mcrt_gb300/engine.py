@@ -164,12 +164,14 @@ _STAGING = {"auto": 0, "shared": 1, "global": 2}
 
 
 def run_opts(precision="fp32", kernel="persistent", seed=1, instance=0, rng_mode=0, photon_begin=0,
-             block_size=0, blocks_per_sm=0, plain_threads=0, table_staging="auto") -> _lib.RunOpts:
+             block_size=0, blocks_per_sm=0, plain_threads=0, table_staging="auto",
+             max_attempts=0) -> _lib.RunOpts:
     """Launch options (mcrt_run_opts). Zero block_size / blocks_per_sm and "auto" staging
-    leave the choice to the library's autotuner."""
+    leave the choice to the library's autotuner; zero max_attempts keeps the default
+    rejection-loop cap (2^20)."""
     return _lib.RunOpts(_PREC[precision], _KERN[kernel], int(seed), int(instance), int(rng_mode),
                         int(photon_begin), int(block_size), int(blocks_per_sm), int(plain_threads),
-                        _STAGING[table_staging])
+                        _STAGING[table_staging], int(max_attempts))
 
 
 def _views(cfg, Irt, Icb, lad):

@@ -215,6 +215,22 @@ def test_edge_cases(M, gpu_ctx, mie5):
         M.simulate(small_cfg(M, g, 10), bad, N0)
 
 
+@pytest.mark.parametrize("prec,kernel", [("fp32", "persistent"), ("fp64", "persistent"), ("fp64", "plain")])
+def test_rejection_cap_is_reported_and_the_context_survives(M, gpu_ctx, prec, kernel):
+    """Failure injected from the host: a rejection-loop cap of one attempt makes every
+    rejected free path hit the cap. The kernel ends those photons, sets
+    MCRT_FLAG_REJECT_LIMIT and returns; the call reports MCRT_ENONCONV; the device stays
+    usable for the next call."""
+    ray = M.RayleighScatterer(0.99, 10.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=0.3 * ray.kl, scatterer=ray)])
+    cfg = small_cfg(M, g, 500)
+    with pytest.raises(M.MCRTError, match="rejection loop hit its iteration cap"):
+        M.simulate(cfg, g, N0, precision=prec, kernel=kernel, seed=3, max_attempts=1)
+    out = M.simulate(cfg, g, N0, precision=prec, kernel=kernel, seed=3, with_extras=True)
+    assert out[7]["stats"]["status_flags"] & 5 == 0
+    assert abs(sum(out[:5]) - 1) < 1e-5
+
+
 def test_full_size_workload_properties(M, gpu_ctx, mie5):
     """At the benchmark workload's size: size-independent properties of the result."""
     g = M.PlaneGeometry(math.radians(150), 0.0, [M.Layer(d=5 * mie5.kl, scatterer=mie5)])
