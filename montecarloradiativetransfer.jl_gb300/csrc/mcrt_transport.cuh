@@ -166,12 +166,34 @@ __device__ void stage_instance(Shared<T, BS>& sh, float4* tables, const KParams&
   __syncthreads();
 }
 
+// The next instance after cur (cyclically) that still has photons to claim, or -1.
 __device__ __forceinline__ int next_instance(const KParams& p, int cur) {
-  for (int i = cur + 1; i < p.n_inst; ++i) {
+  for (int k = 1; k <= p.n_inst; ++k) {
+    const int i = (cur + k) % p.n_inst;
     unsigned long long c = atomicAdd(p.inst[i].claim, 0ull);
     if ((long long)c < p.inst[i].n_photons) return i;
   }
   return -1;
+}
+
+// Where a block starts: blocks are spread over the instances in proportion to their
+// photons (instances come largest first), so a small instance is worked by a few full
+// blocks rather than by every block with a few photons each.
+__device__ __forceinline__ int start_instance(const KParams& p) {
+  double total = 0.0;
+  for (int i = 0; i < p.n_inst; ++i) total += (double)p.inst[i].n_photons;
+  if (!(total > 0.0)) return -1;
+  const double target = (blockIdx.x + 0.5) / gridDim.x * total;
+  double cum = 0.0;
+  int first = p.n_inst - 1;
+  for (int i = 0; i < p.n_inst; ++i) {
+    cum += (double)p.inst[i].n_photons;
+    if (cum > target) {
+      first = i;
+      break;
+    }
+  }
+  return next_instance(p, first - 1 < 0 ? p.n_inst - 1 : first - 1);
 }
 
 __device__ __forceinline__ void acc_add(double* tacc, size_t stride, size_t g, int k, double v) {
@@ -1451,7 +1473,7 @@ __global__ void __launch_bounds__(BS, MINB) k_transport(KParams p) {
   const size_t stride = (size_t)gridDim.x * BS;
 
   if (tid == 0) {
-    sh.cur = next_instance(p, -1);
+    sh.cur = start_instance(p);
     sh.exhausted = 0;
     sh.taken = 0;
     sh.item_next = 0;
