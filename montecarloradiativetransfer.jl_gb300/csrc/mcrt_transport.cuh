@@ -16,13 +16,16 @@
 //    contribution: each lane flushes its bins once per batch with FP64 reductions.
 //    The per-event escaped intensity (the return value of collect_rt_gpu!) is summed
 //    with __shfl_xor_sync across the warp and added per warp into shared memory.
+//    For Rayleigh slabs the RT lanes own polar bins and tally the exact azimuthal
+//    Fourier modes of the peel-off instead (rt_fourier_tile).
 //  * The *finish* phase renormalises each photon by its escaped intensity
 //    (src/gpu.jl:288-291), ends finished paths and claims new photons from the
 //    instance's work queue (a global counter, claimed warp-aggregated).
 //
-// Work: one launch serves any number of instances (simulate() calls); a block works on
-// one instance at a time and moves to the next when the current one has no photons
-// left to claim, so uneven batches run in one persistent launch.
+// Work: one launch serves any number of instances (simulate() calls). Blocks start
+// spread over the instances in proportion to their photons; a block works on one
+// instance at a time and moves on (cyclically) when the current one has no photons left
+// to claim, so uneven batches run in one persistent launch.
 #pragma once
 
 #include <type_traits>
