@@ -6,12 +6,13 @@ driver, running the transport in libmcrt (hand-written CUDA for sm_103a).
 """
 from ._lib import MCRTError, LIB_PATH, lib
 from .engine import (Batch, Context, DeviceMieScatterer, Server, Solve, default_context, run_opts, run_rt, simulate,
-                     write_csv)
+                     simulate_to_stderr, write_csv)
 from .model import (DEFAULT_THEB, Config, Layer, MieScatterer, PlaneGeometry, RayleighScatterer,
                     SphereGeometry, mean_free_path, single_scattering_albedo)
 
 __all__ = [
     "Batch", "Config", "Context", "DEFAULT_THEB", "DeviceMieScatterer", "Layer", "LIB_PATH", "MCRTError", "MieScatterer",
     "PlaneGeometry", "RayleighScatterer", "Server", "Solve", "SphereGeometry", "default_context", "lib",
-    "mean_free_path", "run_opts", "run_rt", "simulate", "single_scattering_albedo", "write_csv",
+    "mean_free_path", "run_opts", "run_rt", "simulate", "simulate_to_stderr", "single_scattering_albedo",
+    "write_csv",
 ]

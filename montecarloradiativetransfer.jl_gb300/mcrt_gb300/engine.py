@@ -260,6 +260,47 @@ class Solve:
             pass
 
 
+def simulate_to_stderr(cfg, g, I0, rel_err: float = 0.01, *, batch: int = 1 << 20, max_photons: int = 1 << 34,
+                       ctx: Optional[Context] = None, **opts):
+    """simulate() until the CB peak (s11 of Icb at θb = 0) is known to ``rel_err``.
+
+    Launches of ``batch`` photons run on consecutive photon ranges of one Philox stream
+    (so the result equals one simulate() of the same total) until the standard error of
+    the per-path CB peak, from its per-path sums of x and x², falls to ``rel_err`` of its
+    mean, or ``max_photons`` have run. Returns ``(result, info)``: ``result`` is
+    simulate()'s tuple for all photons run, ``info`` holds ``photons``, ``rel_err`` and
+    ``launches``."""
+    if rel_err <= 0:
+        raise ValueError("rel_err must be positive")
+    s = Solve(cfg.replace(number_of_rays=batch), g, I0, ctx=ctx, **opts)
+    try:
+        A = Irt = Icb = lad = None
+        n = 0
+        x = x2 = 0.0
+        launches = 0
+        err = math.inf
+        while True:
+            s.launch(n, batch)
+            r = s.read()
+            launches += 1
+            n += batch
+            if A is None:
+                A, Irt, Icb, lad = r["A"], r["Irt"], r["Icb"], r["ladder"]
+            else:
+                A, Irt, Icb, lad = A + r["A"], Irt + r["Irt"], Icb + r["Icb"], lad + r["ladder"]
+            x += r["stats"]["cb_peak_sum"]
+            x2 += r["stats"]["cb_peak_sumsq"]
+            mean = x / n
+            var = max(x2 / n - mean * mean, 0.0)
+            err = math.sqrt(var / n) / mean if mean > 0 else math.inf
+            if err <= rel_err or n + batch > max_photons:
+                break
+    finally:
+        s.close()
+    out = (A[0] / n, A[1] / n, A[2] / n, A[3] / n, A[4] / n, Irt / n, Icb / n)
+    return out, {"photons": n, "rel_err": err, "launches": launches, "ladder": lad / n}
+
+
 class Batch:
     """Many simulate() instances in one persistent launch (per-instance work queues).
 

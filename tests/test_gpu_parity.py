@@ -303,3 +303,19 @@ def test_run_rt_matches_per_state_simulate(M, gpu_ctx, mie5, mie2, geom):
         assert abs(sum(energy.values()) - 1) < 1e-9
     else:
         assert np.all(sm_rt["s11"] > 0)
+
+
+def test_simulate_to_stderr_stops_at_the_target_and_equals_one_run(M, gpu_ctx):
+    """The 1% stopping rule of the CB-peak metric: consecutive launches on one Philox
+    stream until the per-path standard error of the CB peak reaches the target; the sum
+    equals one simulate() of the same photons."""
+    ray = M.RayleighScatterer(0.99, 100.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=3 * ray.kl, scatterer=ray)])
+    cfg = small_cfg(M, g, 1)
+    res, info = M.simulate_to_stderr(cfg, g, N0, rel_err=0.05, batch=2048, precision="fp64", seed=12)
+    assert info["rel_err"] <= 0.05 and info["launches"] >= 1
+    assert info["photons"] == 2048 * info["launches"]
+    one = M.simulate(cfg.replace(number_of_rays=info["photons"]), g, N0, precision="fp64", seed=12)
+    A, Irt, Icb = sim_arrays(res)
+    A1, Irt1, Icb1 = sim_arrays(one)
+    assert scaled_err(A, A1) < 1e-9 and scaled_err(Irt, Irt1) < 1e-9 and scaled_err(Icb, Icb1) < 1e-9
