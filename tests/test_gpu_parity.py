@@ -312,8 +312,8 @@ def test_simulate_to_stderr_stops_at_the_target_and_equals_one_run(M, gpu_ctx):
     ray = M.RayleighScatterer(0.99, 100.0)
     g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=3 * ray.kl, scatterer=ray)])
     cfg = small_cfg(M, g, 1)
-    res, info = M.simulate_to_stderr(cfg, g, N0, rel_err=0.05, batch=2048, precision="fp64", seed=12)
-    assert info["rel_err"] <= 0.05 and info["launches"] >= 1
+    res, info = M.simulate_to_stderr(cfg, g, N0, rel_err=0.02, batch=2048, precision="fp64", seed=12)
+    assert info["rel_err"] <= 0.02 and info["launches"] >= 1
     assert info["photons"] == 2048 * info["launches"]
     one = M.simulate(cfg.replace(number_of_rays=info["photons"]), g, N0, precision="fp64", seed=12)
     A, Irt, Icb = sim_arrays(res)
