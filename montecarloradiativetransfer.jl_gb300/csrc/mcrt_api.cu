@@ -922,8 +922,9 @@ int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const 
   bool warmed = false;
   // Every candidate runs the same photons, so the rates compare steady-state throughput
   // rather than the end-of-launch tail: up to 4 per thread of the largest shape, fewer
-  // when a probe launch (which also warms up the device) shows that a candidate would
-  // take more than about a second.
+  // when a probe launch (which also warms up the device) counts more than 2e11 bin
+  // evaluations for them (about a second). The count, unlike a time, does not change
+  // under a profiler.
   long long ns = std::max<long long>(1, std::min<long long>(nph, 4LL * ctx->sms * 768));
   {
     mcrt_run_opts oo{};
@@ -938,8 +939,12 @@ int autotune(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* g, const 
     if (!build_group(ctx, c, gs, I, &seed, &inst, &n1, photon_begin, rng_mode, 1, &oo, T)) {
       if (launch_group(T) || finish_group(T)) return MCRT_ECUDA;
       warmed = true;
-      const double per_ms = n1 / std::max(T.last_ms, 1e-3f);
-      ns = std::max<long long>(n1, std::min<long long>(ns, (long long)(per_ms * 1000.0)));
+      mcrt_stats st;
+      double Ap[5];
+      if (read_instance(T, 0, Ap, nullptr, nullptr, nullptr, &st)) return MCRT_ECUDA;
+      const double per_photon = (st.rt_evals + st.cb1_evals + st.cbn_evals) / std::max<double>(n1, 1.0);
+      if (per_photon > 0)
+        ns = std::max<long long>(n1, std::min<long long>(ns, (long long)(2e11 / per_photon)));
     }
   }
   auto trial = [&](std::pair<int, int> sh, int st) -> int {
