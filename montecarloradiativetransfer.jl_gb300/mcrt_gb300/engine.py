@@ -4,6 +4,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import json
 import math
 from typing import Dict, List, Optional, Sequence, Tuple
 
@@ -370,12 +371,15 @@ class Server:
 
     ``submit`` queues a simulate() request and returns a ticket; ``result`` waits for it
     and returns ``(A, Irt, Icb, ladder, info)`` divided by the request's photon count,
-    where ``info`` holds the submit / admit / completion times and the waves it took."""
+    where ``info`` holds the submit / admit / completion times and the waves it took.
+    With ``log_path`` every result also appends one JSON line (ticket, photons, latency,
+    queueing time, waves) to that file."""
 
     def __init__(self, *, ctx: Optional[Context] = None, memory_cap_bytes: float = 20e9, max_active: int = 256,
                  wave_photons: int = 1 << 20, min_quantum: int = 4096, precision: str = "fp32",
-                 use_graphs: bool = True):
+                 use_graphs: bool = True, log_path: Optional[str] = None):
         self.ctx = ctx or default_context()
+        self._log = open(log_path, "a", encoding="utf-8") if log_path else None
         o = _lib.ServerOpts(float(memory_cap_bytes), int(max_active), int(wave_photons), int(min_quantum),
                             _PREC[precision], int(use_graphs))
         h = C.c_void_p()
@@ -414,7 +418,13 @@ class Server:
                                        C.byref(info)))
         irt = Irt.reshape(nph, nt, 4).transpose(2, 1, 0)
         icb = Icb.reshape(npb, ntb, 4).transpose(2, 1, 0)
-        return A, irt, icb, lad.reshape(npb, ntb).T, info.as_dict()
+        d = info.as_dict()
+        if self._log:
+            self._log.write(json.dumps({"ticket": int(ticket), "photons": d["photons"], "waves": d["waves"],
+                                        "latency_s": d["completed_s"] - d["submitted_s"],
+                                        "queued_s": d["admitted_s"] - d["submitted_s"]}) + "\n")
+            self._log.flush()
+        return A, irt, icb, lad.reshape(npb, ntb).T, d
 
     def stats(self) -> dict:
         v = np.zeros(8)
@@ -427,6 +437,9 @@ class Server:
         if self.h:
             lib().mcrt_server_destroy(self.h)
             self.h = None
+        if self._log:
+            self._log.close()
+            self._log = None
 
     def __del__(self):
         try:

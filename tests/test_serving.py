@@ -1,6 +1,7 @@
 """The continuous-batching server (mcrt_server_*): results equal simulate(), a request's
 result is the same alone and in a mix, admission respects the memory cap, and graph
 replay equals direct launches."""
+import json
 import math
 
 import numpy as np
@@ -38,9 +39,10 @@ def compare(a, b, tol):
     assert scaled_err(a[2], b[2]) < tol
 
 
-def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2):
+def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2, tmp_path):
     reqs = requests(M, mie5, mie2)[:6]
-    srv = M.Server(precision="fp64", wave_photons=2048, min_quantum=256)
+    log = tmp_path / "serve.jsonl"
+    srv = M.Server(precision="fp64", wave_photons=2048, min_quantum=256, log_path=str(log))
     tickets = [srv.submit(c, g, I, n, seed=s, instance=i) for c, g, I, n, s, i in reqs]
     for t, (c, g, I, n, s, i) in zip(tickets, reqs):
         A, Irt, Icb, lad, info = srv.result(t)
@@ -51,6 +53,8 @@ def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2):
     st = srv.stats()
     assert st["completed"] == len(reqs) and st["resident_bytes"] == 0
     srv.close()
+    lines = [json.loads(x) for x in log.read_text(encoding="utf-8").splitlines()]
+    assert len(lines) == len(reqs) and all(x["latency_s"] >= x["queued_s"] >= 0 for x in lines)
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
