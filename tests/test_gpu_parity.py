@@ -39,6 +39,8 @@ def geometry(M, case, mie5, mie2):
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), [1, 0, 0, -1]
     if case in ("plane_mie_oblique", "plane_mie_short_tau0"):
         return M.PlaneGeometry(math.radians(150), 0.4, [M.Layer(d=3 * mie5.kl, scatterer=mie5)]), [1, 0, 1, 0]
+    if case == "sphere_rayleigh":
+        return M.SphereGeometry(R=3 * ray.kl, scatterer=ray), [1, 0, 0, -1]
     if case == "sphere_mie":
         return M.SphereGeometry(R=6 * mie2.kl, scatterer=mie2), N0
     if case == "two_layers":
@@ -56,7 +58,7 @@ def geometry(M, case, mie5, mie2):
 
 CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite",
          "plane_rayleigh_nphi4", "plane_rayleigh_full_bins", "plane_rayleigh_uneven_phi", "two_layers_rayleigh",
-         "plane_rayleigh_short_tau0", "plane_mie_short_tau0"]
+         "plane_rayleigh_short_tau0", "plane_mie_short_tau0", "sphere_rayleigh"]
 # Bin grids other than small_cfg's. A slab of Rayleigh scatterers tallies RT through
 # azimuthal Fourier modes when Nphi >= 5; Nphi = 4 keeps the per-bin evaluation, and the
 # full grid is the reference's default (64 x 48 RT bins).
