@@ -37,7 +37,7 @@ def geometry(M, case, mie5, mie2):
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), N0
     if case == "plane_rayleigh_V":
         return M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=5 * ray.kl, scatterer=ray)]), [1, 0, 0, -1]
-    if case in ("plane_mie_oblique", "plane_mie_short_tau0"):
+    if case in ("plane_mie_oblique", "plane_mie_short_tau0", "plane_mie_ragged_bins"):
         return M.PlaneGeometry(math.radians(150), 0.4, [M.Layer(d=3 * mie5.kl, scatterer=mie5)]), [1, 0, 1, 0]
     if case == "sphere_rayleigh":
         return M.SphereGeometry(R=3 * ray.kl, scatterer=ray), [1, 0, 0, -1]
@@ -58,7 +58,7 @@ def geometry(M, case, mie5, mie2):
 
 CASES = ["plane_rayleigh", "plane_rayleigh_V", "plane_mie_oblique", "sphere_mie", "two_layers", "semi_infinite",
          "plane_rayleigh_nphi4", "plane_rayleigh_full_bins", "plane_rayleigh_uneven_phi", "two_layers_rayleigh",
-         "plane_rayleigh_short_tau0", "plane_mie_short_tau0", "sphere_rayleigh"]
+         "plane_rayleigh_short_tau0", "plane_mie_short_tau0", "sphere_rayleigh", "plane_mie_ragged_bins"]
 # Bin grids other than small_cfg's. A slab of Rayleigh scatterers tallies RT through
 # azimuthal Fourier modes when Nphi >= 5; Nphi = 4 keeps the per-bin evaluation, and the
 # full grid is the reference's default (64 x 48 RT bins).
@@ -66,7 +66,10 @@ CASE_BINS = {"plane_rayleigh_nphi4": {"Nphi": 4}, "plane_rayleigh_full_bins": {"
              # an irregular azimuth grid: the Fourier tally is expanded at the given angles
              "plane_rayleigh_uneven_phi": {"Nphi": 7, "phi": [0.0, 0.3, 1.1, 2.0, 3.5, 4.4, 6.0]},
              # tau0 below the slab depth: the peel-off and CB cut-offs (t <= tau0) decide many bins
-             "plane_rayleigh_short_tau0": {"tau0": 0.7}, "plane_mie_short_tau0": {"tau0": 0.7}}
+             "plane_rayleigh_short_tau0": {"tau0": 0.7}, "plane_mie_short_tau0": {"tau0": 0.7},
+             # grids that leave lanes and bin pairs partly empty in every tile
+             "plane_mie_ragged_bins": {"Ntheta": 10, "Nphi": 3, "Nphib": 3,
+                                       "thetab": np.deg2rad([0.0, 0.4, 1.1, 1.9, 2.5])}}
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -92,7 +95,7 @@ def test_fp64_kernels_match_oracle_on_same_streams(M, O, gpu_ctx, mie5, mie2, ca
 
 
 @pytest.mark.parametrize("case", ["plane_rayleigh", "plane_mie_oblique", "sphere_mie", "plane_rayleigh_full_bins",
-                                  "plane_mie_short_tau0"])
+                                  "plane_mie_short_tau0", "plane_mie_ragged_bins"])
 def test_fp32_matches_fp64_on_same_streams(M, gpu_ctx, mie5, mie2, case):
     g, I0 = geometry(M, case, mie5, mie2)
     cfg = small_cfg(M, g, 1 << 14, **CASE_BINS.get(case, {}))
