@@ -848,8 +848,10 @@ __device__ __forceinline__ P2 operator*(P2 a, P2 b) { return P2{__fmul2_rn(a.v, 
 __device__ __forceinline__ P2 operator+(P2 a, P2 b) { return P2{__fadd2_rn(a.v, b.v)}; }
 __device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) { return P2{__ffma2_rn(a.v, b.v, c.v)}; }
 
-// acos_as4446 (Abramowitz & Stegun 4.4.46) on two values at once.
-__device__ __forceinline__ P2 acos2(P2 x) {
+// acos_as4446 (Abramowitz & Stegun 4.4.46) on two values at once, times `scale` (the
+// Mie table index per radian): the factor rides on the sign and offset selects, which
+// run on the ALU pipe, instead of costing a multiply on the busy FMA pipe.
+__device__ __forceinline__ P2 acos2_scaled(P2 x, float scale) {
   const P2 ax = p2(fabsf(x.v.x), fabsf(x.v.y));
   P2 p = fma2(p2s(-0.0012624911f), ax, p2s(0.0066700901f));
   p = fma2(p, ax, p2s(-0.0170881256f));
@@ -862,8 +864,9 @@ __device__ __forceinline__ P2 acos2(P2 x) {
   y.v.x = fmaxf(y.v.x, 1e-30f);  // |x| = 1 gives acos = 0 or pi
   y.v.y = fmaxf(y.v.y, 1e-30f);
   const P2 r = (y * p2(rsqrt_approx(y.v.x), rsqrt_approx(y.v.y))) * p;
-  const P2 sg = p2(x.v.x < 0.f ? -1.f : 1.f, x.v.y < 0.f ? -1.f : 1.f);
-  const P2 off = p2(x.v.x < 0.f ? 3.14159265358979f : 0.f, x.v.y < 0.f ? 3.14159265358979f : 0.f);
+  const float pis = 3.14159265358979f * scale;
+  const P2 sg = p2(x.v.x < 0.f ? -scale : scale, x.v.y < 0.f ? -scale : scale);
+  const P2 off = p2(x.v.x < 0.f ? pis : 0.f, x.v.y < 0.f ? pis : 0.f);
   return fma2(sg, r, off);
 }
 
@@ -882,7 +885,7 @@ __device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float
   const P2 A1 = p2s(fct * cD), A3 = p2s(fst * cD), NFST = p2s(-fst), FCT = p2s(fct), SD = p2s(sD);
   const P2 BQ = p2s(fct * sD), NBQ = p2s(-fct * sD), CD = p2s(cD), C4 = p2s(fst * sD);
   const float I0 = E.I[0], I1 = E.I[1], I2 = E.I[2], I3 = E.I[3];
-  const P2 PI0 = p2s(I0), PI1 = p2s(I1), PI2 = p2s(I2), PI3 = p2s(I3);
+  const P2 PI0 = p2s(I0), PI1 = p2s(I1), PI2 = p2s(I2), PI3 = p2s(I3), NPI3 = p2s(-I3);
   const P2 M2I2 = p2s(-2.0f * I2), P2I1 = p2s(2.0f * I1), M1 = p2s(-1.0f), ONE = p2s(1.0f);
   const P2 A = p2s(upper ? E.a_up : E.a_dn);
   P2 QX = p2s(0.f), XZ = p2s(0.f);
@@ -903,24 +906,24 @@ __device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float
     s2.v.y = fmaxf(s2.v.y, 1e-30f);
     const P2 r = p2(rsqrt_approx(s2.v.x), rsqrt_approx(s2.v.y));
     const P2 cpk = k1 * r, spk = k2 * r, stk = s2 * r;
-    const P2 c2 = (cpk + spk) * fma2(spk, M1, cpk);
+    const P2 c2 = fma2(cpk + cpk, cpk, M1);  // cos 2phi = 2 cos^2 - 1 (cpk^2 + spk^2 = 1)
     const P2 srn = spk * cpk;  // -sr / 2
     const P2 q = fma2(c2, PI1, srn * M2I2);
     const P2 u = fma2(c2, PI2, srn * P2I1);
     const P2 cpsi = fma2(spk, BQ, cpk * CD);
     const P2 spsi = fma2(k3, fma2(spk, CD, cpk * NBQ), stk * C4);
-    const P2 c2p = (cpsi + spsi) * fma2(spsi, M1, cpsi);
+    const P2 c2p = fma2(cpsi + cpsi, cpsi, M1);  // cos 2psi (cpsi^2 + spsi^2 = 1)
     const P2 s2p = (spsi * cpsi) * p2s(2.0f);
     P2 p11, p12, p33, p34;
     if (MIE) {
-      const P2 sn = acos2(k3) * p2s(scale);
+      const P2 sn = acos2_scaled(k3, scale);
       int i0 = min((int)sn.v.x, ntheta - 1), i1 = min((int)sn.v.y, ntheta - 1);
       const P2 f = fma2(p2((float)i0, (float)i1), M1, sn);
       const float4 a0 = F[i0], b0 = F[i0 + 1], a1 = F[i1], b1 = F[i1 + 1];
       p11 = fma2(f, p2(b0.x - a0.x, b1.x - a1.x), p2(a0.x, a1.x));
       p12 = fma2(f, p2(b0.y - a0.y, b1.y - a1.y), p2(a0.y, a1.y));
       p33 = fma2(f, p2(b0.z - a0.z, b1.z - a1.z), p2(a0.z, a1.z));
-      p34 = fma2(f, p2(b0.w - a0.w, b1.w - a1.w), p2(a0.w, a1.w));
+      p34 = fma2(f, p2(a0.w - b0.w, a1.w - b1.w), p2(-a0.w, -a1.w));  // holds -p34
     } else {
       const P2 m2 = k3 * k3;
       p11 = fma2(m2, p2s(0.75f), p2s(0.75f));
@@ -932,8 +935,8 @@ __device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float
     const P2 o1 = fma2(p12, PI0, p11 * q);
     P2 o2, o3;
     if (MIE) {
-      o2 = fma2(p33, u, p34 * PI3);
-      o3 = fma2(p33, PI3, (p34 * u) * M1);
+      o2 = fma2(p33, u, p34 * NPI3);  // p34 holds -p34 here
+      o3 = fma2(p34, u, p33 * PI3);
     } else {
       o2 = p33 * u;
       o3 = p33 * PI3;
@@ -1071,7 +1074,7 @@ __device__ __forceinline__ void update_E2(const F2Frame& F, const float E[4], P2
   const P2 br = fma2(p2s(-E[0]), ksp, SE2 * kcp), bi = fma2(p2s(-E[1]), ksp, SE3 * kcp);
   P2 sar, sai, sbr, sbi;
   if (MIE) {
-    const P2 sn = acos2(rz) * p2s(scale);
+    const P2 sn = acos2_scaled(rz, scale);
     const int i0 = min((int)sn.v.x, ntheta - 1), i1 = min((int)sn.v.y, ntheta - 1);
     const P2 f = fma2(p2((float)i0, (float)i1), M1, sn);
     const P2 w0 = fma2(f, M1, p2s(2.0f)), w1 = f + M1;  // the (2 - f, f - 1) weights of mie.jl:80-85
