@@ -406,15 +406,17 @@ def main():
     rt = sum(st["rt_evals"] for st in stats)
     cb1 = sum(st["cb1_evals"] for st in stats)
     cbn = sum(st["cbn_evals"] for st in stats)
-    flops = rt * FLOPS_RT_MIE + cbn * FLOPS_CBN_MIE + cb1 * FLOPS_CB1_MIE
-    achieved = flops / t_dev / 1e12 / world
+    flops = rt * FLOPS_RT_MIE + cbn * FLOPS_CBN_MIE + cb1 * FLOPS_CB1_MIE  # this rank's (one GPU's) work
+    achieved = flops / t_dev / 1e12
     peak = ctx.fp32_peak_tflops()
     traffic = None
     if NCU_DRAM_BYTES_PER_PHOTON is not None:
         traffic = NCU_DRAM_BYTES_PER_PHOTON * B
 
     extras = {}
-    if not args.no_extras:
+    # The extra legs (FP64 forms, CPU baseline, serving, batches, other workloads) run at
+    # N = 1 only: with more ranks the other GPUs would sit idle while rank 0 runs them.
+    if not args.no_extras and world == 1:
         # FP64 forms on bounded samples: the same persistent kernel in FP64, and the plain
         # per-ray FP64 kernel with the reference's structure (denominator of the 5x target).
         n64 = args.fp64_sample
