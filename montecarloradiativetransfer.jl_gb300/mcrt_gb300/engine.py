@@ -262,15 +262,19 @@ class Solve:
 
 
 def simulate_to_stderr(cfg, g, I0, rel_err: float = 0.01, *, batch: int = 1 << 20, max_photons: int = 1 << 34,
-                       ctx: Optional[Context] = None, **opts):
+                       ctx: Optional[Context] = None, state: Optional[dict] = None, **opts):
     """simulate() until the CB peak (s11 of Icb at θb = 0) is known to ``rel_err``.
 
     Launches of ``batch`` photons run on consecutive photon ranges of one Philox stream
     (so the result equals one simulate() of the same total) until the standard error of
     the per-path CB peak, from its per-path sums of x and x², falls to ``rel_err`` of its
     mean, or ``max_photons`` have run. Returns ``(result, info)``: ``result`` is
-    simulate()'s tuple for all photons run, ``info`` holds ``photons``, ``rel_err`` and
-    ``launches``."""
+    simulate()'s tuple for all photons run, ``info`` holds ``photons``, ``rel_err``,
+    ``launches`` and ``state``.
+
+    ``state`` is a checkpoint: the raw sums and the photon count so far (plain numpy
+    values, e.g. for ``numpy.savez``). Passing it back continues the same stream at the
+    next photon, so a stopped run resumes where it left off."""
     if rel_err <= 0:
         raise ValueError("rel_err must be positive")
     s = Solve(cfg.replace(number_of_rays=batch), g, I0, ctx=ctx, **opts)
@@ -278,6 +282,9 @@ def simulate_to_stderr(cfg, g, I0, rel_err: float = 0.01, *, batch: int = 1 << 2
         A = Irt = Icb = lad = None
         n = 0
         x = x2 = 0.0
+        if state is not None:
+            A, Irt, Icb, lad = (np.array(state[k], float) for k in ("A", "Irt", "Icb", "ladder"))
+            n, x, x2 = int(state["photons"]), float(state["peak_sum"]), float(state["peak_sumsq"])
         launches = 0
         err = math.inf
         while True:
@@ -299,7 +306,8 @@ def simulate_to_stderr(cfg, g, I0, rel_err: float = 0.01, *, batch: int = 1 << 2
     finally:
         s.close()
     out = (A[0] / n, A[1] / n, A[2] / n, A[3] / n, A[4] / n, Irt / n, Icb / n)
-    return out, {"photons": n, "rel_err": err, "launches": launches, "ladder": lad / n}
+    ckpt = {"A": A, "Irt": Irt, "Icb": Icb, "ladder": lad, "photons": n, "peak_sum": x, "peak_sumsq": x2}
+    return out, {"photons": n, "rel_err": err, "launches": launches, "ladder": lad / n, "state": ckpt}
 
 
 class Batch:

@@ -324,3 +324,21 @@ def test_simulate_to_stderr_stops_at_the_target_and_equals_one_run(M, gpu_ctx):
     A, Irt, Icb = sim_arrays(res)
     A1, Irt1, Icb1 = sim_arrays(one)
     assert scaled_err(A, A1) < 1e-9 and scaled_err(Irt, Irt1) < 1e-9 and scaled_err(Icb, Icb1) < 1e-9
+
+
+def test_simulate_to_stderr_resumes_from_a_checkpoint(M, gpu_ctx):
+    """A run stopped early and resumed from its checkpoint equals one uninterrupted run."""
+    ray = M.RayleighScatterer(0.99, 100.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=3 * ray.kl, scatterer=ray)])
+    cfg = small_cfg(M, g, 1)
+    _, first = M.simulate_to_stderr(cfg, g, N0, rel_err=1e-9, batch=1024, max_photons=2048,
+                                    precision="fp64", seed=7)
+    assert first["photons"] == 2048
+    saved = {k: np.array(v) for k, v in first["state"].items()}  # what numpy.savez would keep
+    res, info = M.simulate_to_stderr(cfg, g, N0, rel_err=1e-9, batch=1024, max_photons=4096,
+                                     precision="fp64", seed=7, state=saved)
+    assert info["photons"] == 4096
+    one = M.simulate(cfg.replace(number_of_rays=4096), g, N0, precision="fp64", seed=7)
+    A, Irt, Icb = sim_arrays(res)
+    A1, Irt1, Icb1 = sim_arrays(one)
+    assert scaled_err(A, A1) < 1e-9 and scaled_err(Irt, Irt1) < 1e-9 and scaled_err(Icb, Icb1) < 1e-9
