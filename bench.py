@@ -444,6 +444,10 @@ def main():
         serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
         batch = batch_leg(M, ctx)
         others = other_workloads_leg(M, ctx)
+        # the CB peak's standard error from batch means over 32 photon sub-ranges, beside
+        # the per-path estimate on the same photons
+        bm = M.cb_peak_batch_means(cfg, g, I0, batches=32, photons_per_batch=1 << 16, ctx=ctx,
+                                   precision="fp32", seed=3)
         extras = {
             "other_workloads": others,
             "serve": serve,
@@ -487,6 +491,7 @@ def main():
     line.update(extras)
     if "fp64_plain" in extras:
         line["cb_peak"]["seconds_to_1pct_fp64_plain"] = paths_1pct / extras["fp64_plain"]["value"]
+        line["cb_peak"]["batch_means"] = bm
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

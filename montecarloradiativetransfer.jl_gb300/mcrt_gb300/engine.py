@@ -310,6 +310,53 @@ def simulate_to_stderr(cfg, g, I0, rel_err: float = 0.01, *, batch: int = 1 << 2
     return out, {"photons": n, "rel_err": err, "launches": launches, "ladder": lad / n, "state": ckpt}
 
 
+def peak_error_estimates(sums, sumsqs, n_per_batch: int):
+    """Two standard errors of the mean CB peak per path, from ``B`` batches of
+    ``n_per_batch`` paths each, given each batch's sums of x and x² over its paths.
+
+    Batch means: the spread of the ``B`` batch averages, ``std(m_b, ddof=1)/sqrt(B)``.
+    Per path: ``sqrt((Σx²/N − mean²)/N)`` from the pooled sums. For independent paths
+    both estimate the same quantity; their ratio follows ``sqrt(χ²_{B−1}/(B−1))``.
+    Returns ``(mean, se_batch_means, se_per_path)``."""
+    s = np.asarray(sums, float)
+    ss = np.asarray(sumsqs, float)
+    if s.ndim != 1 or s.shape != ss.shape or s.size < 2 or n_per_batch < 1:
+        raise ValueError("need at least two batches of equal, positive size")
+    n_total = s.size * n_per_batch
+    mean = float(s.sum()) / n_total
+    se_bm = float(np.std(s / n_per_batch, ddof=1)) / math.sqrt(s.size)
+    var = max(float(ss.sum()) / n_total - mean * mean, 0.0)
+    return mean, se_bm, math.sqrt(var / n_total)
+
+
+def cb_peak_batch_means(cfg, g, I0, *, batches: int = 32, photons_per_batch: int = 1 << 16,
+                        ctx: Optional[Context] = None, **opts) -> dict:
+    """The CB peak's standard error from batch means over ``batches`` independent photon
+    sub-ranges (consecutive ranges of one Philox stream), beside the per-path estimate
+    from the same photons' sums of x and x². Returns a dict with the mean per path, both
+    relative errors, and the paths each implies for a 1% relative standard error."""
+    if batches < 2:
+        raise ValueError("batch means need at least two batches")
+    s = Solve(cfg.replace(number_of_rays=photons_per_batch), g, I0, ctx=ctx, **opts)
+    sums, sqs = [], []
+    try:
+        for b in range(batches):
+            s.launch(b * photons_per_batch, photons_per_batch)
+            st = s.read()["stats"]
+            sums.append(st["cb_peak_sum"])
+            sqs.append(st["cb_peak_sumsq"])
+    finally:
+        s.close()
+    mean, se_bm, se_pp = peak_error_estimates(sums, sqs, photons_per_batch)
+    n = batches * photons_per_batch
+    out = {"batches": batches, "photons_per_batch": photons_per_batch, "mean_per_path": mean}
+    for name, se in (("batch_means", se_bm), ("per_path", se_pp)):
+        rel = se / mean if mean > 0 else math.inf
+        out["rel_err_" + name] = rel
+        out["paths_for_1pct_" + name] = n * (rel / 0.01) ** 2
+    return out
+
+
 class Batch:
     """Many simulate() instances in one persistent launch (per-instance work queues).
 

@@ -342,3 +342,18 @@ def test_simulate_to_stderr_resumes_from_a_checkpoint(M, gpu_ctx):
     A, Irt, Icb = sim_arrays(res)
     A1, Irt1, Icb1 = sim_arrays(one)
     assert scaled_err(A, A1) < 1e-9 and scaled_err(Irt, Irt1) < 1e-9 and scaled_err(Icb, Icb1) < 1e-9
+
+
+def test_cb_peak_batch_means_agree_with_the_per_path_error(M, gpu_ctx):
+    """The CB peak's standard error from batch means over 32 photon sub-ranges against
+    the per-path estimate: their ratio follows sqrt(chi2_31 / 31), inside [0.39, 1.77]
+    with probability 1 - 2e-8. The sub-ranges tile one stream, so the mean equals one
+    simulate() of all their photons."""
+    ray = M.RayleighScatterer(0.99, 100.0)
+    g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=3 * ray.kl, scatterer=ray)])
+    cfg = small_cfg(M, g, 1)
+    r = M.cb_peak_batch_means(cfg, g, N0, batches=32, photons_per_batch=2048, precision="fp64", seed=4)
+    mu = r["mean_per_path"]
+    assert mu > 0 and 0.39 < r["rel_err_batch_means"] / r["rel_err_per_path"] < 1.77
+    one = M.simulate(cfg.replace(number_of_rays=32 * 2048), g, N0, precision="fp64", seed=4)
+    assert abs(mu - one[6][0, 0, 0]) < 1e-9 * mu

@@ -224,3 +224,22 @@ def test_csv_writer_uses_the_reference_columns(M, tmp_path):
     assert head[:3] == ["θ", "ϕ", "s11"] and head[-1] == "s44" and len(head) == 18
     row = [float(v) for v in lines[2].split(",")]
     assert row[0] == 20.0 and row[2] == pytest.approx(-1.1) and row[-1] == pytest.approx(-4.4)
+
+
+def test_peak_error_estimates_batch_means_and_per_path_agree(M):
+    """The two standard errors of the CB peak agree on independent draws: their ratio
+    follows sqrt(chi2_31 / 31), inside [0.46, 1.64] with probability 1 - 2e-6. A
+    hand-computed case pins the formulas."""
+    rng = np.random.default_rng(3)
+    x = rng.exponential(2.0, size=(32, 4096))
+    mean, se_bm, se_pp = M.peak_error_estimates(x.sum(1), (x * x).sum(1), 4096)
+    assert abs(mean - x.mean()) < 1e-12
+    assert 0.46 < se_bm / se_pp < 1.64
+    assert abs(se_pp - x.std() / math.sqrt(x.size)) < 1e-12 * se_pp
+    # two batches of two paths: x = (1, 3 | 5, 7)
+    mean, se_bm, se_pp = M.peak_error_estimates([4.0, 12.0], [10.0, 74.0], 2)
+    assert mean == 4.0
+    assert abs(se_bm - np.std([2.0, 6.0], ddof=1) / math.sqrt(2)) < 1e-15
+    assert abs(se_pp - math.sqrt((84.0 / 4 - 16.0) / 4)) < 1e-15
+    with pytest.raises(ValueError):
+        M.peak_error_estimates([1.0], [1.0], 10)

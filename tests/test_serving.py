@@ -3,6 +3,7 @@ result is the same alone and in a mix, admission respects the memory cap, and gr
 replay equals direct launches."""
 import json
 import math
+import time
 
 import numpy as np
 import pytest
@@ -43,6 +44,7 @@ def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2, tmp_path):
     reqs = requests(M, mie5, mie2)[:6]
     log = tmp_path / "serve.jsonl"
     srv = M.Server(precision="fp64", wave_photons=2048, min_quantum=256, log_path=str(log))
+    t0 = time.perf_counter()
     tickets = [srv.submit(c, g, I, n, seed=s, instance=i) for c, g, I, n, s, i in reqs]
     for t, (c, g, I, n, s, i) in zip(tickets, reqs):
         A, Irt, Icb, lad, info = srv.result(t)
@@ -50,8 +52,11 @@ def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2, tmp_path):
         compare((A, Irt, Icb), (np.array(solo[:5]), solo[5], solo[6]), 1e-9)
         assert info["photons"] == n and info["waves"] >= 1
         assert info["submitted_s"] <= info["admitted_s"] <= info["completed_s"]
+    wall = time.perf_counter() - t0
     st = srv.stats()
     assert st["completed"] == len(reqs) and st["resident_bytes"] == 0
+    # waves overlap on two streams; busy time is the union of their intervals
+    assert 0 < st["busy_s"] <= wall
     srv.close()
     lines = [json.loads(x) for x in log.read_text(encoding="utf-8").splitlines()]
     assert len(lines) == len(reqs) and all(x["latency_s"] >= x["queued_s"] >= 0 for x in lines)
