@@ -33,6 +33,34 @@ def cb_peak_stats(stats):
     return mu, math.sqrt(var)
 
 
+# ------------------------------------------------------------------ reciprocity
+def reciprocity_z(run, costheta, n_batches):
+    """Plane-slab reciprocity R(mu, mu0, phi) = R(mu0, mu, phi) for unpolarised light.
+
+    ``run(theta, seed)`` returns ``(cfg, Irt)`` for incidence zenith ``theta`` (propagation
+    azimuth 0), Irt of shape (4, Ntheta, Nphi) divided by the photon count. Incidence is
+    put at each upward Gauss-Legendre node of ``costheta``. The reflection function is
+    Irt[0] / (inorm mu): the normalisation under which the single-scattering result
+    omega P11 [1 - exp(-tau (1/mu0 + 1/mu))] / (mu + mu0) is symmetric. Returns the
+    z-scores of R(a -> b, phi_k) - R(b -> a, phi_k) over every node pair and azimuth, from
+    batch means over independent seeds."""
+    up = np.where(np.asarray(costheta) > 0)[0]
+    R = {}
+    for i in up:
+        batches = []
+        for k in range(n_batches):
+            cfg, irt = run(math.pi - math.acos(costheta[i]), 1000 * int(i) + k)
+            batches.append(irt[0] / (cfg.inorm[:, None] * cfg.costheta[:, None]))
+        b = np.array(batches)
+        R[i] = (b.mean(0), b.std(0, ddof=1) / math.sqrt(n_batches))
+    z = []
+    for a in up:
+        for b in up:
+            if a < b:
+                z.extend(((R[a][0][b] - R[b][0][a]) / np.hypot(R[a][1][b], R[b][1][a])).tolist())
+    return np.array(z)
+
+
 # ------------------------------------------------------------------ run_rt restatement
 # The checker for mcrt_run_rt: the Mueller assembly of src/MonteCarloRadiativeTransfer.jl
 # :87-291 in numpy, fed by one simulate-like call per incident state. ``sim(I, i)``
