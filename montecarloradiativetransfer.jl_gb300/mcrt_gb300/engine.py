@@ -548,13 +548,35 @@ def run_rt(cfg, g, *, use_gpu: bool = True, ctx: Optional[Context] = None, with_
     return sm_rt, sm_cb, energy
 
 
-def write_csv(table: dict, path: str) -> None:
-    """Writes a run_rt table (the reference's DataFrame columns ``θ, ϕ, s11 .. s44``,
-    src/MonteCarloRadiativeTransfer.jl:176-182, 280-290) as CSV with those headers."""
-    cols = [k for k in ("theta", "phi") if k in table] + [f"s{a}{b}" for a in range(1, 5) for b in range(1, 5)]
+def _table_columns(table: dict):
+    """The reference's DataFrame columns of a run_rt table, in order: ``θ`` (and ``ϕ`` for
+    a plane), then ``s11 .. s44`` (src/MonteCarloRadiativeTransfer.jl:176-182, 280-290).
+    Returns ``[(header, float64 array)]``."""
+    keys = [k for k in ("theta", "phi") if k in table] + [f"s{a}{b}" for a in range(1, 5) for b in range(1, 5)]
     names = {"theta": "θ", "phi": "ϕ"}
-    data = np.column_stack([np.asarray(table[c], float) for c in cols])
+    return [(names.get(k, k), np.asarray(table[k], float)) for k in keys]
+
+
+def write_csv(table: dict, path: str) -> None:
+    """Writes a run_rt table as CSV with the reference's DataFrame headers ``θ, ϕ, s11 .. s44``."""
+    cols = _table_columns(table)
+    data = np.column_stack([v for _, v in cols])
     with open(path, "w", encoding="utf-8") as f:
-        f.write(",".join(names.get(c, c) for c in cols) + "\n")
+        f.write(",".join(h for h, _ in cols) + "\n")
         for row in data:
             f.write(",".join(repr(float(v)) for v in row) + "\n")
+
+
+def write_arrow(table: dict, path: str) -> None:
+    """Writes a run_rt table as an Arrow IPC file (readable as a DataFrame by Arrow.jl or
+    pandas) with the reference's column names ``θ, ϕ, s11 .. s44``, all Float64. Needs
+    pyarrow, which is imported only here."""
+    try:
+        import pyarrow as pa
+        import pyarrow.ipc as ipc
+    except ImportError as e:  # the CSV writer needs nothing
+        raise ImportError("write_arrow needs pyarrow; write_csv writes the same table without it") from e
+    cols = _table_columns(table)
+    t = pa.table({h: pa.array(v, type=pa.float64()) for h, v in cols})
+    with pa.OSFile(path, "wb") as sink, ipc.new_file(sink, t.schema) as w:
+        w.write_table(t)

@@ -243,3 +243,20 @@ def test_peak_error_estimates_batch_means_and_per_path_agree(M):
     assert abs(se_pp - math.sqrt((84.0 / 4 - 16.0) / 4)) < 1e-15
     with pytest.raises(ValueError):
         M.peak_error_estimates([1.0], [1.0], 10)
+
+
+def test_arrow_writer_uses_the_reference_columns(M, tmp_path):
+    pa = pytest.importorskip("pyarrow")
+    import pyarrow.ipc as ipc
+
+    tab = {"theta": np.array([10.0, 20.0])}  # a sphere table has no phi column
+    for a in range(1, 5):
+        for b in range(1, 5):
+            tab[f"s{a}{b}"] = np.array([a + 0.1 * b, -(a + 0.1 * b)])
+    p = tmp_path / "rt.arrow"
+    M.write_arrow(tab, str(p))
+    with pa.memory_map(str(p)) as src:
+        t = ipc.open_file(src).read_all()
+    assert t.column_names == ["θ"] + [f"s{a}{b}" for a in range(1, 5) for b in range(1, 5)]
+    assert all(f.type == pa.float64() for f in t.schema)
+    assert t.column("θ").to_pylist() == [10.0, 20.0] and t.column("s44").to_pylist() == [4.4, -4.4]
