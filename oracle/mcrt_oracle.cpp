@@ -11,8 +11,9 @@
 // the reference cannot be run here. The restatement is instead pinned by known-answer
 // tests derived from the reference's semantics: published Philox4x32-10 vectors,
 // exact per-photon energy closure, the analytic single-scattering slab reflection,
-// the Rayleigh sampler's density, an independent Mie evaluation, and agreement of the
-// reference's O(n) reciprocal-path walk with the incremental form.
+// the Rayleigh sampler's density, an independent Mie evaluation, agreement of the
+// reference's O(n) reciprocal-path walk with the incremental form, and reciprocity of
+// the slab reflection function at the 3-sigma level.
 //
 // Random numbers: the reference calls an unseeded rand(). Here every draw comes from
 // Philox4x32-10 keyed by (seed, instance) with counter (photon, event, attempt), and
