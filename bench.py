@@ -245,14 +245,22 @@ def other_workloads_leg(M, ctx, n32=1 << 16, n64=1 << 12):
     return out
 
 
-def cpu_oracle_rate(M, n_sample, threads=0):
+def oracle_workload(O, n_rays):
+    """The same workload built from the oracle's own types (its own bhmie and Config), so
+    that the CPU legs never load the library."""
+    mie = O.MieScatterer(5.0 / (2 * math.pi), 1.5 + 0.001j, 1.0, 0.1, Ntheta=1801)
+    g = O.PlaneGeometry(math.radians(150.0), 0.0, [O.Layer(d=5.0 * mie.kl, scatterer=mie)])
+    return mie, g, O.Config(g, number_of_rays=n_rays)
+
+
+def cpu_oracle_rate(n_sample, threads=0):
     """Times the oracle (the FP64 C++ restatement of the reference's CPU path) on a bounded
     sample of the same workload with all host threads."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if os.path.join(ROOT, "oracle") not in sys.path:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    mie, g, cfg = workload(M, n_sample)
-    O.lib()
+    mie, g, cfg = oracle_workload(O, n_sample)
     t0 = time.perf_counter()
     O.simulate(cfg, g, [1.0, 0.0, 0.0, 0.0], seed=11, threads=threads)
     dt = time.perf_counter() - t0
@@ -262,16 +270,16 @@ def cpu_oracle_rate(M, n_sample, threads=0):
 
 def run_reference(args, rank):
     """The reference arm: the reference's CPU algorithm (as the FP64 C++ oracle port,
-    since Julia is not installed) on the host's cores, same workload and metric."""
+    since Julia is not installed) on the host's cores, same workload and metric. It
+    loads only the oracle: its Mie tables and Config come from the oracle's own
+    restatement of the reference."""
     if rank != 0:
         return
-    import mcrt_gb300 as M
-
     rates = []
     for _ in range(max(args.warmup, 0)):
-        cpu_oracle_rate(M, max(args.cpu_sample // 4, 100))
+        cpu_oracle_rate(max(args.cpu_sample // 4, 100))
     for _ in range(args.steps):
-        r, cores, dt = cpu_oracle_rate(M, args.cpu_sample)
+        r, cores, dt = cpu_oracle_rate(args.cpu_sample)
         rates.append(r)
     v = float(np.mean(rates))
     line = {
@@ -283,7 +291,8 @@ def run_reference(args, rank):
                          "sample": f"{args.cpu_sample} photons per step of the same workload"},
         "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "Julia is not installed here, so the reference's CPU path runs as its FP64 C++ "
-                "restatement (oracle/mcrt_oracle.cpp) with OpenMP over photons",
+                "restatement (oracle/mcrt_oracle.cpp) with OpenMP over photons; the Mie tables come "
+                "from the oracle's own bhmie, and the library is not loaded",
     }
     print(json.dumps(line), flush=True)
 
@@ -440,7 +449,7 @@ def main():
         sp.close()
         v64 = np64 / (r64["stats"]["kernel_ms"] / 1e3)
         vplain = n64 / (rp["stats"]["kernel_ms"] / 1e3)
-        cpu_v, cores, cpu_dt = cpu_oracle_rate(M, args.cpu_sample)
+        cpu_v, cores, cpu_dt = cpu_oracle_rate(args.cpu_sample)
         serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
         batch = batch_leg(M, ctx)
         others = other_workloads_leg(M, ctx)

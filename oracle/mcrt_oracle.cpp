@@ -1126,6 +1126,138 @@ double orc_kepler_solver(double M, double e) {
   return kepler_solver(M, e, &capped);
 }
 
-int orc_version(void) { return 1; }
+// MieScatterer's tables (src/scatterers/mie.jl:36-44): bhmie (mie.jl:129-216) for the
+// amplitude functions S1, S2 and the normalised Mueller elements F11, F12, F33, F34 on
+// Nθ uniform angles over [0, π], then calculate_csrn (src/utils.jl:263-287) for the
+// inverse CDF of cos(Θ) on random_points + 1 uniform probabilities. S1, S2 are
+// interleaved (re, im). q = {q_ext, q_sca, q_abs, q_back, asymm}. Returns 0, or 1 for
+// invalid sizes.
+int orc_mie_tables(double x, double m_re, double m_im, int n_theta, int random_points, double* F11,
+                   double* F12, double* F33, double* F34, double* S1_out, double* S2_out, double* csrn,
+                   double* q) {
+  if (!(x > 0) || n_theta < 2 || random_points < 1) return 1;
+  const cplx m(m_re, m_im);
+  const cplx y = m * x;
+  const int nstop = (int)std::floor(std::max(x + 4 * std::cbrt(x) + 2, x * std::abs(m)));  // mie.jl:133
+  const int nmax = nstop + 15;                                                             // nextra = 15
+  const int N = n_theta;
+  // θ = range(0, π, Nθ); μ = cos.(θ). Arrays below are 1-based as in the reference.
+  std::vector<double> mu(N + 1);
+  for (int i = 1; i <= N; ++i) mu[i] = std::cos(PI * (double)(i - 1) / (double)(N - 1));
+  std::vector<cplx> d(nmax + 1, cplx(0.0, 0.0));  // d[nmax] = 0; downward recursion (mie.jl:138-141)
+  for (int n = nmax - 1; n >= 1; --n) d[n] = (double)(n + 1) / y - 1.0 / (d[n + 1] + (double)(n + 1) / y);
+  std::vector<double> pin(N + 1, 0.0), tn(N + 1, 0.0), pi0(N + 1, 0.0), pi1(N + 1, 1.0);
+  std::vector<cplx> S1(N + 1, cplx(0.0, 0.0)), S2(N + 1, cplx(0.0, 0.0));
+  double psi0 = std::cos(x), psi1 = std::sin(x), chi0 = -std::sin(x), chi1 = std::cos(x);
+  cplx xi1(psi1, -chi1), a_prev(0.0, 0.0), b_prev(0.0, 0.0);
+  double qsca = 0.0, g = 0.0;
+  for (int n = 1; n <= nstop; ++n) {
+    const double dn = (double)n;
+    const double fn = (2.0 * dn + 1.0) / (dn * (dn + 1.0));
+    const double psi = (2.0 * dn - 1.0) * psi1 / x - psi0;
+    const double chi = (2.0 * dn - 1.0) * chi1 / x - chi0;
+    const cplx xi(psi, -chi);
+    const cplx da = d[n] / m + dn / x, db = d[n] * m + dn / x;
+    const cplx an = (da * psi - psi1) / (da * xi - xi1);  // mie.jl:163-165
+    const cplx bn = (db * psi - psi1) / (db * xi - xi1);
+    qsca += (std::norm(an) + std::norm(bn)) * (2.0 * dn + 1.0);
+    g += (an.real() * bn.real() + an.imag() * bn.imag()) * fn;
+    if (n > 1)
+      g += (a_prev.real() * an.real() + a_prev.imag() * an.imag() + b_prev.real() * bn.real() +
+            b_prev.imag() * bn.imag()) * (dn - 1.0) * (dn + 1.0) / dn;
+    for (int i = 1; i <= (N + 1) / 2; ++i) {  // mie.jl:173-184: half range, mirrored by parity
+      const int ii = N + 1 - i;
+      pin[i] = pi1[i];
+      tn[i] = dn * mu[i] * pin[i] - (dn + 1.0) * pi0[i];
+      S1[i] += fn * (an * pin[i] + bn * tn[i]);
+      S2[i] += fn * (an * tn[i] + bn * pin[i]);
+      if (i < ii) {
+        const double p = (n & 1) == 0 ? -1.0 : 1.0;
+        S1[ii] += fn * (an * pin[i] - bn * tn[i]) * p;
+        S2[ii] += fn * (-an * tn[i] + bn * pin[i]) * p;
+      }
+    }
+    psi0 = psi1;
+    psi1 = psi;
+    chi0 = chi1;
+    chi1 = chi;
+    xi1 = cplx(psi1, -chi1);
+    a_prev = an;
+    b_prev = bn;
+    for (int i = 1; i <= N; ++i) pi1[i] = ((2.0 * dn + 1.0) * mu[i] * pin[i] - (dn + 1.0) * pi0[i]) / dn;
+    for (int i = 1; i <= N; ++i) pi0[i] = pin[i];
+  }
+  g *= 2.0 / qsca;
+  qsca *= 2.0 / (x * x);
+  const double qext = 4.0 / (x * x) * S1[1].real();
+  if (q) {
+    q[0] = qext;
+    q[1] = qsca;
+    q[2] = qext - qsca;
+    q[3] = 4.0 / (x * x) * std::norm(S1[N]);
+    q[4] = g;
+  }
+  const double coeff = 4.0 / (qsca * x * x);  // mie.jl:201-212
+  for (int i = 1; i <= N; ++i) {
+    const double s1 = std::norm(S1[i]), s2 = std::norm(S2[i]);
+    const cplx c = S2[i] * std::conj(S1[i]);
+    F11[i - 1] = (s1 + s2) * 0.5 * coeff;
+    F12[i - 1] = -(s1 - s2) * 0.5 * coeff;
+    F33[i - 1] = c.real() * coeff;
+    F34[i - 1] = c.imag() * coeff;
+    S1_out[2 * (i - 1)] = S1[i].real();
+    S1_out[2 * (i - 1) + 1] = S1[i].imag();
+    S2_out[2 * (i - 1)] = S2[i].real();
+    S2_out[2 * (i - 1) + 1] = S2[i].imag();
+  }
+
+  // calculate_csrn(itpf11, n) with itpf11 the linear interpolant of F11 on the θ grid.
+  const int n = random_points;
+  const double hstep = PI / (double)(N - 1);
+  auto itp11 = [&](double t) {  // linear_interpolation(range(0, π, Nθ), F11)
+    double s = t / hstep;
+    int j = (int)std::floor(s);
+    if (j < 0) j = 0;
+    if (j > N - 2) j = N - 2;
+    const double w = s - j;
+    return (1.0 - w) * F11[j] + w * F11[j + 1];
+  };
+  std::vector<double> xv(n + 1), yv(n + 1);
+  double run = 0.0;
+  for (int i = 0; i <= n; ++i) {  // xv = (0:n) ./ (n / π); yv = cumsum(itp11(xv) .* sin.(xv))
+    xv[i] = (double)i / ((double)n / PI);
+    run += itp11(xv[i]) * std::sin(xv[i]);
+    yv[i] = run;
+  }
+  const double total = yv[n];
+  for (int i = 0; i <= n; ++i) {
+    xv[i] = PI - xv[i];
+    yv[i] = 1.0 - yv[i] / total;
+  }
+  // swap roles: knots are the probabilities, values the cosines; then reverse both
+  std::vector<double> kx(n + 1), ky(n + 1);
+  for (int i = 0; i <= n; ++i) {
+    kx[n - i] = yv[i];
+    ky[n - i] = -std::cos(xv[i]);
+  }
+  // linear_interpolation(xv[2:end], yv[2:end]) evaluated at ex = (0:n) ./ n; the first
+  // reversed knot duplicates the second (sin π rounds the last increment away)
+  for (int j = 0; j <= n; ++j) {
+    const double e = (double)j / (double)n;
+    int lo = 1, hi = n;  // knots kx[1..n]; find the last k with kx[k] <= e, clamped to [1, n-1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (kx[mid] <= e) lo = mid;
+      else hi = mid;
+    }
+    int k = lo;
+    if (k > n - 1) k = n - 1;
+    const double w = (e - kx[k]) / (kx[k + 1] - kx[k]);
+    csrn[j] = (1.0 - w) * ky[k] + w * ky[k + 1];
+  }
+  return 0;
+}
+
+int orc_version(void) { return 2; }
 
 }  // extern "C"

@@ -1,13 +1,19 @@
-"""ctypes binding of the CPU oracle (oracle/mcrt_oracle.cpp).
+"""ctypes binding of the CPU oracle (oracle/mcrt_oracle.cpp) and the oracle's own
+restatement of the reference's input types.
 
 TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline use it as the checker; the library and its Python host code never do.
-Parity is unpinned by the reference (it ships no golden vectors and Julia is not
-installed); see the header of mcrt_oracle.cpp for how the oracle is pinned instead.
+baseline and reference arm use it as the checker; the library and its Python host
+code never do. This module imports nothing from the library: the Mie tables come from
+the oracle's own bhmie / calculate_csrn (orc_mie_tables), and Config, the geometries and
+the scatterers are restated here from src/config.jl, src/geometries/*.jl and
+src/scatterers/*.jl. Parity is unpinned by the reference (it ships no golden vectors
+and Julia is not installed); see the header of mcrt_oracle.cpp for how the oracle is
+pinned instead.
 """
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -71,6 +77,8 @@ def lib() -> C.CDLL:
         L.orc_rayleigh_sample.restype = C.c_double
         L.orc_kepler_solver.argtypes = [C.c_double, C.c_double]
         L.orc_kepler_solver.restype = C.c_double
+        L.orc_mie_tables.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int, C.c_int] + [_dp] * 8
+        L.orc_mie_tables.restype = C.c_int
         _lib = L
     return _lib
 
@@ -156,3 +164,140 @@ def simulate(cfg, g, I0, *, seed=1, instance=0, rng_mode=0, cb_form=0, threads=0
         "counters": dict(zip(["events", "attempts", "rt_evals", "cb1_evals", "cbn_evals", "kepler_capped",
                               "attempts_capped"], ct)),
     }
+
+
+# ------------------------------------------------------------------ reference input types
+# Restated from the reference, independently of the library's host package, so that the
+# oracle and the reference arm build their inputs without loading the library.
+
+RAYLEIGH, MIE = 0, 1
+PLANE, SPHERE = 0, 1
+
+# DEFAULT_THEB of src/config.jl:3-53, in degrees.
+DEFAULT_THEB_DEG = [0.0, 0.02, 0.04, 0.06, 0.08, 0.1, 0.15, 0.2, 0.25, 0.3, 0.35, 0.4, 0.45, 0.5, 0.6, 0.7,
+                    0.8, 0.9, 1.0, 1.5, 2.0, 2.5, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0, 12.0, 15.0, 18.0, 21.0,
+                    24.0, 27.0, 30.0, 40.0, 50.0, 60.0, 70.0, 80.0, 90.0, 100.0, 110.0, 120.0, 130.0, 140.0,
+                    150.0, 160.0, 170.0, 180.0]
+
+
+def mie_tables(x, m, n_theta=181, random_points=1000):
+    """bhmie (src/scatterers/mie.jl:129-216) and calculate_csrn (src/utils.jl:263-287) in
+    the oracle: dict with F11, F12, F33, F34, S11, S22 (complex), csrn, q_ext, q_sca,
+    q_abs, q_back, asymm."""
+    n, rp = int(n_theta), int(random_points)
+    F = [np.zeros(n) for _ in range(4)]
+    S = [np.zeros(2 * n) for _ in range(2)]
+    cs = np.zeros(rp + 1)
+    q = np.zeros(5)
+    m = complex(m)
+    rc = lib().orc_mie_tables(float(x), m.real, m.imag, n, rp, *[_p(f) for f in F], _p(S[0]), _p(S[1]),
+                              _p(cs), _p(q))
+    if rc != 0:
+        raise ValueError("orc_mie_tables: invalid arguments")
+    out = dict(zip(("F11", "F12", "F33", "F34"), F))
+    out["S11"] = S[0][0::2] + 1j * S[0][1::2]
+    out["S22"] = S[1][0::2] + 1j * S[1][1::2]
+    out["csrn"] = cs
+    out.update(zip(("q_ext", "q_sca", "q_abs", "q_back", "asymm"), (float(v) for v in q)))
+    return out
+
+
+class RayleighScatterer:
+    """RayleighScatterer(ω, kl) (src/scatterers/rayleigh.jl:3-6)."""
+
+    kind = RAYLEIGH
+
+    def __init__(self, omega, kl):
+        self.omega, self.kl = float(omega), float(kl)
+
+
+class MieScatterer:
+    """MieScatterer(r, m, λ, ν; Nθ=181, random_points=1000) (src/scatterers/mie.jl:36-44):
+    x = 2πr/λ, ω = q_sca/q_ext, kl = (4/3 r)/(ν q_ext), tables from the oracle's bhmie."""
+
+    kind = MIE
+
+    def __init__(self, r, m, lam=1.0, nu=0.1, *, Ntheta=181, random_points=1000):
+        self.r, self.m, self.lam, self.nu = float(r), complex(m), float(lam), float(nu)
+        self.x = 2 * math.pi * self.r / self.lam
+        t = mie_tables(self.x, self.m, Ntheta, random_points)
+        self.q_ext, self.q_sca, self.q_abs, self.q_back, self.asymm = (
+            t["q_ext"], t["q_sca"], t["q_abs"], t["q_back"], t["asymm"])
+        self.omega = self.q_sca / self.q_ext
+        self.kl = (4.0 / 3.0) * self.r / (self.nu * self.q_ext)
+        self.F11, self.F12, self.F33, self.F34 = t["F11"], t["F12"], t["F33"], t["F34"]
+        self.S11, self.S22, self.csrn = t["S11"], t["S22"], t["csrn"]
+        self.Ntheta, self.random_points = int(Ntheta), int(random_points)
+
+    def rounded_fp32(self):
+        """A view with every table rounded to FP32, as a device that stores FP32 tables sees it."""
+        f = lambda a: np.asarray(a, np.float32).astype(np.float64)
+        c = lambda z: f(z.real) + 1j * f(z.imag)
+        o = MieScatterer.__new__(MieScatterer)
+        o.__dict__.update(self.__dict__)
+        o.F11, o.F12, o.F33, o.F34 = f(self.F11), f(self.F12), f(self.F33), f(self.F34)
+        o.S11, o.S22, o.csrn = c(self.S11), c(self.S22), f(self.csrn)
+        return o
+
+
+class Layer:
+    """Layer(d, n=1, scatterer, τ=d/kl, ω) (src/geometries/plane.jl:6-21); d < 0 is a
+    semi-infinite layer."""
+
+    def __init__(self, d, scatterer, n=1.0, tau=None, omega=None):
+        self.d, self.scatterer, self.n = float(d), scatterer, float(n)
+        self.tau = float(tau) if tau is not None else self.d / scatterer.kl
+        self.omega = float(omega) if omega is not None else scatterer.omega
+        self.infinite = self.d < 0
+
+
+class PlaneGeometry:
+    """PlaneGeometry(θ, ϕ, layers) (src/geometries/plane.jl:28-38)."""
+
+    kind = PLANE
+
+    def __init__(self, theta, phi, layers):
+        self.theta, self.phi, self.layers = float(theta), float(phi), list(layers)
+
+    def initial_weights(self, Ntheta, Nphi):  # plane.jl:131-142, half-range Gauss-Legendre
+        h = Ntheta // 2
+        x, w = np.polynomial.legendre.leggauss(h)
+        cos = np.concatenate([(x - 1.0) / 2.0, -((x - 1.0) / 2.0)[::-1]])
+        inorm = np.concatenate([w / 2.0, (w / 2.0)[::-1]]) * (1.0 / (2 * Nphi))
+        return cos, np.sqrt(1.0 - cos ** 2), inorm
+
+
+class SphereGeometry:
+    """SphereGeometry(R, n=1, scatterer, τ=R/kl, ω) (src/geometries/sphere.jl:6-21)."""
+
+    kind = SPHERE
+    theta, phi = math.pi, 0.0
+
+    def __init__(self, R, scatterer, n=1.0, tau=None, omega=None):
+        self.R, self.scatterer, self.n = float(R), scatterer, float(n)
+        self.tau = float(tau) if tau is not None else self.R / scatterer.kl
+        self.omega = float(omega) if omega is not None else scatterer.omega
+
+    def initial_weights(self, Ntheta, Nphi):  # sphere.jl:85-90
+        cos, w = np.polynomial.legendre.leggauss(Ntheta)
+        return cos, np.sqrt(1.0 - cos ** 2), w / (2 * Nphi)
+
+
+class Config:
+    """Config (src/config.jl:55-124): the reference's defaults and derived trig tables."""
+
+    def __init__(self, geometry, *, number_of_rays=1000, minimum_intensity=1e-6, maximum_scattering_times=10000,
+                 compute_cb=True, tau0=50.0, Nphi=48, Ntheta=64, thetab=None, Nphib=8):
+        self.number_of_rays = int(number_of_rays)
+        self.minimum_intensity = float(minimum_intensity)
+        self.maximum_scattering_times = int(maximum_scattering_times)
+        self.compute_cb, self.tau0 = bool(compute_cb), float(tau0)
+        self.Nphi, self.Ntheta, self.Nphib = int(Nphi), int(Ntheta), int(Nphib)
+        phi = np.linspace(0.0, 2 * math.pi * (self.Nphi - 1) / self.Nphi, self.Nphi)  # config.jl:81
+        self.cosphi, self.sinphi = np.cos(phi), np.sin(phi)
+        self.costheta, self.sintheta, self.inorm = geometry.initial_weights(self.Ntheta, self.Nphi)
+        tb = np.asarray(thetab, float) if thetab is not None else math.pi / 180.0 * np.array(DEFAULT_THEB_DEG)
+        self.Nthetab = len(tb)
+        self.costhetab, self.sinthetab = np.cos(tb), np.sin(tb)
+        phib = np.linspace(0.0, 2 * math.pi * (self.Nphib - 1) / self.Nphib, self.Nphib)  # config.jl:117
+        self.cosphib, self.sinphib = np.cos(phib), np.sin(phib)

@@ -38,13 +38,24 @@ def gpu_ctx(M):
     return M.default_context()
 
 
-@pytest.fixture(scope="session")
-def mie5(M):
-    """Mie spheres x = 5, m = 1.5 + 0.001i, 1801-angle tables."""
-    return M.MieScatterer(5.0 / (2 * math.pi), 1.5 + 0.001j, 1.0, 0.1, Ntheta=1801)
+def oracle_made_mie(M, O, x, m):
+    """A library scatterer whose tables come from the oracle's own bhmie and calculate_csrn
+    (as the Julia binding hands the library the tables that the reference's MieScatterer
+    made), so that parity runs feed both sides one producer's tables and the library's
+    producer is checked on its own against the oracle's."""
+    o = O.MieScatterer(x / (2 * math.pi), m, 1.0, 0.1, Ntheta=1801)
+    s = M.MieScatterer.from_tables(o.omega, o.kl, o.F11, o.F12, o.F33, o.F34, o.S11, o.S22, o.csrn)
+    s.r, s.m, s.lam, s.nu, s.x, s.q_ext = o.r, o.m, o.lam, o.nu, o.x, o.q_ext
+    return s
 
 
 @pytest.fixture(scope="session")
-def mie2(M):
-    """Mie spheres x = 2, m = 1.31, 1801-angle tables."""
-    return M.MieScatterer(2.0 / (2 * math.pi), 1.31 + 0.0j, 1.0, 0.1, Ntheta=1801)
+def mie5(M, O):
+    """Mie spheres x = 5, m = 1.5 + 0.001i, 1801-angle tables (made by the oracle)."""
+    return oracle_made_mie(M, O, 5.0, 1.5 + 0.001j)
+
+
+@pytest.fixture(scope="session")
+def mie2(M, O):
+    """Mie spheres x = 2, m = 1.31, 1801-angle tables (made by the oracle)."""
+    return oracle_made_mie(M, O, 2.0, 1.31 + 0.0j)

@@ -40,3 +40,20 @@ def test_gpu_arm_fails_loudly_without_a_device(M):
     assert r.returncode != 0
     assert r.stdout.strip() == ""
     assert "no CUDA device is visible" in r.stderr
+
+
+def test_reference_arm_does_not_load_the_library():
+    """The reference arm builds its workload from the oracle's own types and Mie tables:
+    the process never imports the library's package nor maps libmcrt.so."""
+    code = (
+        "import sys, runpy\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', '--cpu-sample', '8']\n"
+        "runpy.run_path('bench.py', run_name='__main__')\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'mcrt_gb300' not in sys.modules, 'package imported'\n"
+        "assert 'libmcrt.so' not in maps, 'libmcrt.so mapped'\n"
+        "assert 'libmcrt_oracle.so' in maps\n"
+        "print('checked')\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().endswith("checked")

@@ -183,3 +183,53 @@ def test_plane_reflection_is_reciprocal(M, O):
     z = reciprocity_z(run, _small_cfg(M, _plane(M, ray, 1.0), 1).costheta, 16)
     assert z.size == 224
     assert np.max(np.abs(z)) < 5.0 and np.mean(np.abs(z) > 3.0) < 0.03
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_oracle_mie_tables_match_an_independent_mie_evaluation(O, case):
+    """The oracle's own bhmie (mie.jl:129-216) against the scipy Riccati-Bessel golden."""
+    c = json.load(open(os.path.join(GOLDEN, "mie_scipy.json")))[case]
+    x, m = c["x"], complex(*c["m"])
+    t = O.mie_tables(x, m, n_theta=7)
+    assert abs(t["q_ext"] / c["q_ext"] - 1) < 1e-10
+    assert abs(t["q_sca"] / c["q_sca"] - 1) < 1e-10
+    assert abs(t["asymm"] / c["asymm"] - 1) < 1e-9
+    S1 = np.array([complex(*v) for v in c["S1"]])
+    S2 = np.array([complex(*v) for v in c["S2"]])
+    assert np.max(np.abs(t["S11"] - S1)) < 1e-10 * np.max(np.abs(S1))
+    assert np.max(np.abs(t["S22"] - S2)) < 1e-10 * np.max(np.abs(S2))
+
+
+@pytest.mark.parametrize("x,m", [(5.0, 1.5 + 0.001j), (2.0, 1.31 + 0j), (0.5, 1.3 + 1e-5j), (10.0, 1.6 + 0.01j)])
+def test_oracle_and_library_mie_producers_agree(M, O, x, m):
+    """The oracle's MieScatterer (its own bhmie + calculate_csrn, no library code) and the
+    library's host producer give the same albedo, mean free path and tables."""
+    r = x / (2 * math.pi)
+    o = O.MieScatterer(r, m, 1.0, 0.1, Ntheta=1801)
+    p = M.MieScatterer(r, m, 1.0, 0.1, Ntheta=1801)
+    assert abs(o.omega - p.omega) < 1e-12 and abs(o.kl / p.kl - 1) < 1e-12
+    for k in ("F11", "F12", "F33", "F34", "S11", "S22", "csrn"):
+        a, b = getattr(o, k), getattr(p, k)
+        assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b)), k
+    # calculate_csrn: the inverse CDF of cos(theta) under F11 sin(theta)
+    th = np.linspace(0, math.pi, 1801)
+    assert np.all(np.diff(o.csrn) >= 0) and o.csrn[-1] == 1.0
+    assert abs(np.trapezoid(o.F11 * np.sin(th), th) / 2 - 1) < 1e-4
+
+
+def test_oracle_config_mirrors_the_library_config(M, O):
+    """The oracle's Config (config.jl:55-124, plane.jl:131-142, sphere.jl:85-90) equals the
+    library host package's on the same geometry."""
+    ro, rp = O.RayleighScatterer(0.99, 100.0), M.RayleighScatterer(0.99, 100.0)
+    pairs = [(O.PlaneGeometry(2.6, 0.1, [O.Layer(d=500.0, scatterer=ro)]),
+              M.PlaneGeometry(2.6, 0.1, [M.Layer(d=500.0, scatterer=rp)]), {}),
+             (O.SphereGeometry(R=300.0, scatterer=ro), M.SphereGeometry(R=300.0, scatterer=rp),
+              {"Ntheta": 20, "Nphi": 7, "Nphib": 3, "thetab": [0.0, 0.01, 0.02]})]
+    for go, gp, kw in pairs:
+        co, cp = O.Config(go, **kw), M.Config(gp, **kw)
+        assert (co.Ntheta, co.Nphi, co.Nthetab, co.Nphib) == (cp.Ntheta, cp.Nphi, cp.Nthetab, cp.Nphib)
+        for k in ("cosphi", "sinphi", "costheta", "sintheta", "inorm", "costhetab", "sinthetab", "cosphib",
+                  "sinphib"):
+            assert np.array_equal(getattr(co, k), getattr(cp, k)), k
+        taus = (go.tau, gp.tau) if go.kind == O.SPHERE else (go.layers[0].tau, gp.layers[0].tau)
+        assert taus[0] == taus[1]
