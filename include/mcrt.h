@@ -314,13 +314,18 @@ int mcrt_server_destroy(mcrt_server* s);
  * the caller's scatterers (created beforehand with mcrt_scatterer_create) lives in one
  * file-scope device array of MCRT_NOALLOC_SCRATCH_BYTES bytes, which every GPU that
  * loads the library holds until the process exits: the instance descriptor, the bin
- * tables, the tallies, the work counters and the photon-state pool. It runs one block
- * per SM, so it is slower than mcrt_simulate.
+ * tables, the tallies, the work counters and the photon-state pool.
  *
+ * - The array is created on a device, and the kernels this call launches are loaded
+ *   there, when the first context on that device is created (mcrt_ctx_create looks up
+ *   the array's device address with that device current). A caller that reserves the
+ *   device's memory itself creates its context, and its scatterers, before it does.
+ * - It runs one block per SM (256 threads in FP32, 128 in FP64, Mie tables staged in
+ *   shared memory), so it is slower than mcrt_simulate. In opts, block_size must be 0
+ *   or that size, blocks_per_sm 0 or 1, table_staging 0 or 1, and kernel the persistent
+ *   one; other values are rejected with MCRT_EINVAL.
  * - A config whose bin tables and tallies do not fit in the array beside the
  *   photon-state pool is rejected with MCRT_EINVAL and a message giving both sizes.
- * - The first call on a device looks up the array's device address; make that first
- *   call before any stream capture on that device.
  * - Every call reuses the same array: each call clears the tallies and counters it
  *   needs before its launch, and calls that overlap on the GPU (from several threads or
  *   contexts on one device) race on the array and must be serialised by the caller. */

@@ -93,6 +93,7 @@ struct mcrt_ctx {
     double paths_per_ms;
   };
   std::map<std::string, Tuned> tuned;  // workload signature -> fastest launch shape
+  unsigned char* noalloc_scratch = nullptr;  // device address of mcrt_simulate_noalloc's array
 };
 
 struct mcrt_scatterer {
@@ -131,6 +132,10 @@ int mcrt_device_count(void) {
   return n;
 }
 
+namespace {
+int noalloc_prepare(mcrt_ctx* ctx);
+}
+
 int mcrt_ctx_create(int device, mcrt_ctx** out) {
   if (!out) return set_err(MCRT_EINVAL, "mcrt_ctx_create: out is NULL");
   *out = nullptr;
@@ -145,6 +150,10 @@ int mcrt_ctx_create(int device, mcrt_ctx** out) {
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&c->e0));
   CK(cudaEventCreate(&c->e1));
+  // Everything mcrt_simulate_noalloc needs on the device is made resident now, so that
+  // its calls allocate nothing even where modules load lazily.
+  int rc = noalloc_prepare(c.get());
+  if (rc) return rc;
   *out = c.release();
   return MCRT_OK;
 }
@@ -1896,6 +1905,25 @@ int noalloc_base(int device, unsigned char** out) {
   return MCRT_OK;
 }
 
+// The launch shape of mcrt_simulate_noalloc: one block per SM of this many threads.
+int noalloc_block_size(int prec) { return prec == MCRT_FP32 ? 256 : 128; }
+
+// Called by mcrt_ctx_create with the context's device current. Looking up the array's
+// address loads the module that holds it (and so creates the array on the device where
+// modules load lazily); querying the two kernels it launches loads theirs. Afterwards a
+// call allocates nothing on the device.
+int noalloc_prepare(mcrt_ctx* ctx) {
+  int rc = noalloc_base(ctx->device, &ctx->noalloc_scratch);
+  if (rc) return rc;
+  for (int prec : {MCRT_FP32, MCRT_FP64}) {
+    KInfo ki;
+    if (!kernel_info(prec, noalloc_block_size(prec), ki)) return set_err(MCRT_EINVAL, "no kernel for this precision");
+    cudaFuncAttributes fa;
+    CK(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(ki.fn)));
+  }
+  return MCRT_OK;
+}
+
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
 // The bin tables of upload_bins laid out at a given device address, as host bytes.
@@ -1967,10 +1995,18 @@ extern "C" int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, cons
     return set_err(MCRT_EINVAL, "precision must be MCRT_FP32 or MCRT_FP64");
   if (opts && opts->kernel != MCRT_KERNEL_PERSISTENT)
     return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc runs the persistent kernel only");
+  const int bs = noalloc_block_size(prec);
+  if (opts && opts->block_size != 0 && opts->block_size != bs)
+    return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc runs 256 threads per block (FP32) or 128 (FP64); "
+                                "block_size must be 0 or that value");
+  if (opts && opts->blocks_per_sm != 0 && opts->blocks_per_sm != 1)
+    return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc runs one block per SM; blocks_per_sm must be 0 or 1");
+  if (opts && opts->table_staging != 0 && opts->table_staging != 1)
+    return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc stages Mie tables in shared memory; table_staging "
+                                "must be 0 or 1");
   CK(cudaSetDevice(ctx->device));
-  unsigned char* base = nullptr;
-  rc = noalloc_base(ctx->device, &base);
-  if (rc) return rc;
+  unsigned char* base = ctx->noalloc_scratch;
+  if (!base) return set_err(MCRT_EINVAL, "mcrt_simulate_noalloc: the context has no scratch array");
 
   DevInstance D;
   host::Sph kfs;
@@ -1981,16 +2017,20 @@ extern "C" int mcrt_simulate_noalloc(mcrt_ctx* ctx, const mcrt_config* cfg, cons
   HostBins H = make_bins(cfg, g->kind, kfs);
 
   // Launch shape: one block per SM.
-  const int bs = prec == MCRT_FP32 ? 256 : 128;
   KInfo ki;
   if (!kernel_info(prec, bs, ki)) return set_err(MCRT_EINVAL, "no kernel for this precision");
   int tf4 = table_f4_of(D);
   size_t smem = ki.shared_static + (size_t)tf4 * 16;
   if (smem > (size_t)ctx->smem_optin) {
-    tf4 = (int)((ctx->smem_optin - ki.shared_static) / 16);
+    // the tables that do not fit are read from global memory through L1
+    tf4 = (int)(((long long)ctx->smem_optin - (long long)ki.shared_static) / 16);
+    if (tf4 < 0) return set_err(MCRT_EINVAL, "block size too large for shared memory");
     smem = ki.shared_static + (size_t)tf4 * 16;
   }
   CK(cudaFuncSetAttribute(ki.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ki.fn, bs, smem));
+  if (occ < 1) return set_err(MCRT_EINVAL, "kernel does not fit on an SM with this block size");
   const int blocks = ctx->sms;
   const size_t slots = (size_t)blocks * bs;
 

@@ -122,3 +122,52 @@ def table_of(M, plane):
     """The s_ab columns of an assembled matrix in run_rt's row order (theta fastest)."""
     return {f"s{a + 1}{b + 1}": (M[a, b].reshape(-1, order="F") if plane else M[a, b])
             for a in range(4) for b in range(4)}
+
+
+def tally_scale(b):
+    """The scale of scaled_err: the largest |I| of a Stokes tally, else the largest |b|."""
+    b = np.asarray(b, float)
+    return float(np.max(np.abs(b[0]))) if b.ndim == 3 and b.shape[0] == 4 else float(np.max(np.abs(b)))
+
+
+def per_element_err(a, b, floor_frac):
+    """Per-element relative error max |a - b| / |b| over the elements with
+    |b| >= floor_frac * scale (scale as in scaled_err). Returns (max error, elements
+    compared, elements in the tally, the floor)."""
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    floor = floor_frac * tally_scale(b)
+    m = np.abs(b) >= floor
+    if not np.any(m):
+        return 0.0, 0, int(b.size), floor
+    return float(np.max(np.abs(a[m] - b[m]) / np.abs(b[m]))), int(m.sum()), int(b.size), floor
+
+
+def independent_stream_z(batches, ref_sum, n_ref, n_per_batch, min_samples=16.0):
+    """z-scores of a tally from independent streams: GPU batch means (``batches`` of shape
+    (nb, ...) divided by ``n_per_batch``) against the oracle's raw sum over ``n_ref``
+    photons. The oracle's standard error comes from the same per-path variance (the
+    batches' spread scaled to n_ref paths), as both sample one distribution under the
+    hypothesis tested.
+
+    Only elements that the oracle samples well enough for a normal approximation are
+    scored: for a Stokes tally of shape (4, ...), a bin counts when the oracle's relative
+    standard error of its intensity (component 0) is at most 1 / sqrt(min_samples), that
+    is, when its photons carry the equivalent of min_samples or more independent
+    contributions; rarer bins (grazing peel-off directions that only events within a
+    fraction of a mean free path of the surface reach) are Poisson-limited at the
+    oracle's sample size. Returns (z of the scored elements, scored bins, all bins)."""
+    B = np.asarray(batches, float)
+    nb = B.shape[0]
+    mean = B.mean(0)
+    sd = B.std(0, ddof=1)
+    se_gpu = sd / math.sqrt(nb)
+    se_ref = sd * math.sqrt(n_per_batch / n_ref)
+    se = np.sqrt(se_gpu ** 2 + se_ref ** 2)
+    ref = np.asarray(ref_sum, float) / n_ref
+    I = mean[0] if (mean.ndim == 3 and mean.shape[0] == 4) else mean
+    seI = se_ref[0] if (mean.ndim == 3 and mean.shape[0] == 4) else se_ref
+    ok = (np.abs(I) > 0) & (seI <= np.abs(I) / math.sqrt(min_samples))
+    mask = np.broadcast_to(ok, mean.shape) & (se > 0)
+    z = np.abs(mean - ref)[mask] / se[mask]
+    return z, int(ok.sum()), int(ok.size)

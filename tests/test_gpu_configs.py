@@ -1,0 +1,129 @@
+"""GPU parity on the benchmark configurations at their own parameters and bin grids:
+
+  * Rayleigh slab: omega 0.99, kl 100, tau 10, normal incidence, Ntheta 180, 200 CB
+    phase angles over 0-2 degrees, Nphi 48, Nphi_b 8, at most 1000 orders;
+  * Mie slab: x 5, m 1.5+0.001i, 1801-angle tables, tau 5, incidence zenith 30 degrees,
+    the reference's default grids (Ntheta 64, Nphi 48, 51 CB angles, Nphi_b 8);
+  * Mie sphere: tau 20, x 2, m 1.31, 500 CB phase angles over 0-5 degrees, default
+    Ntheta and Nphi.
+
+For each, three comparisons against the oracle (the CPU restatement of the reference's
+src/cpu.jl:162-273, with the CB bin body of src/gpu.jl:41-175):
+  (a) the FP64 persistent and FP64 plain kernels on identical Philox streams: 1e-9 of
+      the tally scale on every element of every tally, and 1e-8 relative on every
+      element above 1e-6 of the scale;
+  (b) the FP32 kernel against the FP64 kernel on identical streams at >= 1e5 photons:
+      1e-4 of the tally scale on every tally, and the per-element relative error stated
+      above a floor of 1e-3 of the scale (gated at 2e-3; the values are printed);
+  (c) independent streams, GPU batch means (16 batches) against the oracle: every
+      well-sampled Stokes element of Irt and Icb within 3 combined standard errors,
+      allowing the 1% that a 3-sigma band misses by chance and none beyond 5.5 sigma,
+      and the CB enhancement factor within 3 sigma.
+
+The Mie tables come from the oracle's own bhmie and calculate_csrn (tests/conftest.py).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import independent_stream_z, per_element_err, scaled_err, sim_arrays
+
+pytestmark = pytest.mark.gpu
+N0 = [1.0, 0.0, 0.0, 0.0]
+
+
+def workload(M, name, mie5, mie2, n):
+    if name == "rayleigh_slab":
+        ray = M.RayleighScatterer(0.99, 100.0)
+        g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=10.0 * ray.kl, scatterer=ray)])
+        return g, M.Config(g, number_of_rays=n, Ntheta=180, thetab=np.deg2rad(np.linspace(0.0, 2.0, 200)),
+                           maximum_scattering_times=1000)
+    if name == "mie_slab":
+        g = M.PlaneGeometry(math.radians(150.0), 0.0, [M.Layer(d=5.0 * mie5.kl, scatterer=mie5)])
+        return g, M.Config(g, number_of_rays=n)
+    if name == "mie_sphere":
+        g = M.SphereGeometry(R=20.0 * mie2.kl, scatterer=mie2)
+        return g, M.Config(g, number_of_rays=n, thetab=np.deg2rad(np.linspace(0.0, 5.0, 500)))
+    raise ValueError(name)
+
+
+NAMES = ["rayleigh_slab", "mie_slab", "mie_sphere"]
+# photons of the identical-stream comparison: persistent kernel, plain kernel (one
+# thread per photon, FP64: the long Rayleigh-slab and sphere paths keep it short)
+SAME_STREAM = {"rayleigh_slab": (128, 32), "mie_slab": (512, 128), "mie_sphere": (128, 32)}
+# independent streams: (GPU photons per batch, oracle photons)
+INDEPENDENT = {"rayleigh_slab": (1 << 14, 1024), "mie_slab": (1 << 16, 8192), "mie_sphere": (1 << 14, 768)}
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fp64_kernels_match_the_oracle_on_identical_streams(M, O, gpu_ctx, mie5, mie2, name):
+    n_pers, n_plain = SAME_STREAM[name]
+    for kernel, n in (("persistent", n_pers), ("plain", n_plain)):
+        g, cfg = workload(M, name, mie5, mie2, n)
+        ref = O.simulate(cfg, g, N0, seed=31, threads=0)
+        out = M.simulate(cfg, g, N0, precision="fp64", kernel=kernel, seed=31, with_extras=True)
+        A, Irt, Icb = sim_arrays(out)
+        st = out[7]["stats"]
+        assert st["status_flags"] & 5 == 0 and st["photons"] == n
+        assert st["events"] == ref["counters"]["events"], (kernel, st["events"], ref["counters"]["events"])
+        pairs = {"A": (A, ref["A"] / n), "Irt": (Irt, ref["Irt"] / n), "Icb": (Icb, ref["Icb"] / n),
+                 "ladder": (out[7]["ladder"], ref["ladder"] / n)}
+        for k, (a, b) in pairs.items():
+            assert scaled_err(a, b) < 1e-9, (name, kernel, k, scaled_err(a, b))
+            e, used, total, _ = per_element_err(a, b, 1e-6)
+            assert e < 1e-8, (name, kernel, k, e, used, total)
+        assert abs(st["cb_peak_sum"] / ref["stats"]["cb_peak_sum"] - 1) < 1e-9
+        assert abs(A.sum() - 1) < 1e-12
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fp32_matches_fp64_on_identical_streams_at_1e5_photons(M, gpu_ctx, mie5, mie2, name):
+    n = 1 << 17
+    g, cfg = workload(M, name, mie5, mie2, n)
+    o64 = M.simulate(cfg, g, N0, precision="fp64", seed=7, with_extras=True)
+    o32 = M.simulate(cfg, g, N0, precision="fp32", seed=7, with_extras=True)
+    A64, R64, C64 = sim_arrays(o64)
+    A32, R32, C32 = sim_arrays(o32)
+    pairs = {"A": (A32, A64), "Irt": (R32, R64), "Icb": (C32, C64), "ladder": (o32[7]["ladder"], o64[7]["ladder"])}
+    report = {}
+    for k, (a, b) in pairs.items():
+        e, used, total, floor = per_element_err(a, b, 1e-3)
+        report[k] = {"scaled": scaled_err(a, b), "per_element_max": e, "elements": f"{used}/{total}"}
+    print(name, "FP32 vs FP64 on identical streams,", n, "photons:", report)
+    for k, r in report.items():
+        assert r["scaled"] < 1e-4, (name, k, r)
+        assert r["per_element_max"] < 2e-3, (name, k, r)
+    assert abs(A32.sum() - 1) < 1e-5
+    assert o32[7]["stats"]["status_flags"] & 5 == 0
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_statistics_agree_with_the_oracle_on_independent_streams(M, O, gpu_ctx, mie5, mie2, name):
+    n_b, n_ref = INDEPENDENT[name]
+    nb = 16
+    g, cfg = workload(M, name, mie5, mie2, n_b)
+    s = M.Solve(cfg, g, N0, precision="fp32", seed=101)
+    R, Cb, L = [], [], []
+    for b in range(nb):
+        s.launch(b * n_b, n_b)
+        r = s.read()
+        R.append(r["Irt"] / n_b)
+        Cb.append(r["Icb"] / n_b)
+        L.append(r["ladder"] / n_b)
+    s.close()
+    R, Cb, L = np.array(R), np.array(Cb), np.array(L)
+    ref = O.simulate(cfg.replace(number_of_rays=n_ref), g, N0, seed=202, threads=0)
+    for tally, batches, key in (("Irt", R, "Irt"), ("Icb", Cb, "Icb")):
+        z, scored, bins = independent_stream_z(batches, ref[key], n_ref, n_b)
+        print(name, tally, f"{scored}/{bins} bins scored, max z {z.max():.2f}, beyond 3 sigma {np.mean(z > 3):.4f}")
+        assert scored >= 0.5 * bins, (name, tally, scored, bins)
+        assert np.mean(z > 3) < 0.01, (name, tally, np.mean(z > 3))
+        assert z.max() < 5.5, (name, tally, z.max())
+    # CB enhancement at exact backscatter: s11 of Icb over the incoherent ladder at theta_b = 0
+    enh = Cb[:, 0, 0, 0] / L[:, 0, 0]
+    enh_ref = ref["Icb"][0, 0, 0] / ref["ladder"][0, 0]
+    se = enh.std(ddof=1) * math.sqrt(1.0 / nb + n_b / n_ref)
+    print(name, f"CB enhancement GPU {enh.mean():.5f} oracle {enh_ref:.5f} (se {se:.5f})")
+    assert abs(enh.mean() - enh_ref) < 3 * se
+    assert 1.0 < enh_ref <= 2.0 and 1.0 < enh.mean() <= 2.0
