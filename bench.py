@@ -5,7 +5,8 @@ Workload (one GPU): Mie spheres of size parameter 5 and refractive index 1.5+0.0
 (1801-angle tables stored in FP32), a plane slab of optical thickness 5 with the Mie
 albedo, incidence zenith angle 30 degrees, unpolarised light, the reference's default
 bin grids, FP32 transport with FP64 CB phase reduction and FP64 tallies. One step is
-one persistent launch over a batch of photons; the full workload is 1e8 photons.
+one persistent launch over a batch of photons (2^22 by default); the workload's full
+size is 1e8 photons, and the line's config states the photons actually timed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -32,7 +33,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "montecarloradiativetransfer.jl_gb300"))
 
 WORKLOAD = "mie_x5_m1.5+0.001i_slab_tau5_zenith30"
-TOTAL_PHOTONS = 100_000_000
+FULL_WORKLOAD_PHOTONS = 100_000_000  # the workload's stated size; the line reports what was timed
 # Algorithmic flops per bin evaluation of the reference's algorithm for a Mie
 # scatterer: additions + multiplications (FMA = 2), special functions (div, sqrt, exp,
 # sin/cos, acos) not counted. They come from the oracle's per-bin arithmetic
@@ -67,7 +68,7 @@ def parse():
     ap.add_argument("--case-workload", default="mie_slab", choices=["mie_slab", "rayleigh_slab", "mie_sphere"],
                     help="workload of --case: the Mie slab, the Rayleigh slab (tau 10, Ntheta 180, 200 "
                          "CB angles) or the Mie sphere (tau 20, x 2, 500 CB angles)")
-    ap.add_argument("--serve-requests", type=int, default=256)
+    ap.add_argument("--serve-requests", type=int, default=4096)
     ap.add_argument("--serve-scale", type=float, default=1e-3, help="photon budget multiplier of the stream")
     return ap.parse_args()
 
@@ -175,12 +176,14 @@ def serve_leg(M, ctx, n_req, scale, rate_hz=200.0, seed=5):
             "memory_cap_bytes": 20e9}
 
 
-def batch_leg(M, ctx, n_inst=256, scale=1e-3, seed=4):
+def batch_leg(M, ctx, n_inst=256, scale=1.5e-2, seed=4):
     """One persistent launch over uneven slab instances drawn like the 256-instance batch
     (optical thickness log-uniform in [0.1, 50], albedo uniform in [0.5, 0.9999], Rayleigh
     or Mie with x in U[0.5, 10], n in U[1.3, 1.6], k log-uniform in [1e-5, 1e-2] on 1801
     angles, photon budgets lognormal(median 1e7, sigma 1)) with the budgets multiplied by
-    `scale`."""
+    `scale` (1.5e-2: 5.7e7 paths for this seed, a launch of about 30 s; the full budgets
+    total 3.8e9 paths). Creating the batch autotunes
+    its launch shape on a sample of its photons, so the one launch timed here is warm."""
     rng = np.random.default_rng(seed)
     insts = []
     ray_cache = None
@@ -201,25 +204,49 @@ def batch_leg(M, ctx, n_inst=256, scale=1e-3, seed=4):
     b = M.Batch(cfg, insts, ctx=ctx, precision="fp32")
     b.launch()
     ms, photons = b.timing()
-    b.launch()
-    ms, photons = b.timing()
     b.close()
     return {"instances": n_inst, "budget_scale": scale, "photons": photons, "kernel_ms": ms,
             "paths_per_s": photons / (ms / 1e3)}
 
 
+def _scale(b):
+    """The largest |I| of a Stokes tally (shape (4, ...)), else the largest |b|."""
+    b = np.asarray(b, float)
+    return float(np.max(np.abs(b[0]))) if b.ndim >= 2 and b.shape[0] == 4 else float(np.max(np.abs(b)))
+
+
 def _scaled_err(a, b):
     """max |a - b| over the largest |I| of b (Stokes tallies of shape (4, ...))."""
     a, b = np.asarray(a, float), np.asarray(b, float)
-    scale = np.max(np.abs(b[0])) if b.ndim >= 2 and b.shape[0] == 4 else np.max(np.abs(b))
+    scale = _scale(b)
     return float(np.max(np.abs(a - b)) / scale) if scale > 0 else float(np.max(np.abs(a)))
 
 
-def other_workloads_leg(M, ctx, n32=1 << 16, n64=1 << 12):
+ERR_FLOOR = 1e-3  # per-element errors are stated on the elements with |b| >= ERR_FLOOR * scale
+
+
+def _fp32_err(a, b):
+    """FP32-against-FP64 error of one tally: the scaled error, and the per-element relative
+    error |a - b| / |b| over the elements above ERR_FLOOR of the tally's scale."""
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    m = np.abs(b) >= ERR_FLOOR * _scale(b)
+    pe = float(np.max(np.abs(a[m] - b[m]) / np.abs(b[m]))) if np.any(m) else 0.0
+    return {"scaled": _scaled_err(a, b), "per_element_max": pe, "elements": int(m.sum()), "of": int(b.size)}
+
+
+def _fp32_errs(r32, r64):
+    out = {k: _fp32_err(r32[k], r64[k]) for k in ("A", "Irt", "Icb", "ladder")}
+    out["floor"] = ERR_FLOOR
+    return out
+
+
+def other_workloads_leg(M, ctx, n32=1 << 16, n64=None):
     """The Rayleigh slab (Nθ = 180, 200 CB angles over 0-2°, τ = 10, ω = 0.99, normal
-    incidence) and the Mie sphere (τ = 20, x = 2, m = 1.31, 500 CB angles over 0-5°) at
-    bounded sizes: FP32 paths/s, FP64 paths/s, and the FP32-vs-FP64 scaled error of
-    every tally on identical Philox streams."""
+    incidence, at most 1000 orders) and the Mie sphere (τ = 20, x = 2, m = 1.31, 500 CB
+    angles over 0-5°): FP32 paths/s, FP64 paths/s, and the FP32-vs-FP64 error of every
+    tally on identical Philox streams. FP64 runs at about 1/64 of the FP32 rate on this
+    GPU, so its samples are 2^14 (slab) and 2^13 (sphere) photons."""
+    n64 = n64 or {"rayleigh_slab_tau10": 1 << 14, "mie_sphere_tau20": 1 << 13}
     I0 = [1.0, 0.0, 0.0, 0.0]
     ray = M.RayleighScatterer(0.99, 100.0)
     g1 = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=10 * ray.kl, scatterer=ray)])
@@ -233,14 +260,18 @@ def other_workloads_leg(M, ctx, n32=1 << 16, n64=1 << 12):
     out = {}
     for name, g, mk, seed in runs:
         r32 = M.simulate(mk(n32), g, I0, ctx=ctx, precision="fp32", seed=seed, with_extras=True)
-        a = M.simulate(mk(n64), g, I0, ctx=ctx, precision="fp32", seed=seed + 100, with_extras=True)
-        b = M.simulate(mk(n64), g, I0, ctx=ctx, precision="fp64", seed=seed + 100, with_extras=True)
+        n = n64[name]
+        res = {}
+        for prec in ("fp32", "fp64"):
+            s = M.Solve(mk(n), g, I0, ctx=ctx, precision=prec, seed=seed + 100)
+            s.launch(0, n)
+            res[prec] = s.read()
+            s.close()
         out[name] = {
             "fp32_paths_per_s": n32 / (r32[7]["stats"]["kernel_ms"] / 1e3), "fp32_photons": n32,
-            "fp64_paths_per_s": n64 / (b[7]["stats"]["kernel_ms"] / 1e3), "fp64_photons": n64,
+            "fp64_paths_per_s": n / (res["fp64"]["stats"]["kernel_ms"] / 1e3), "fp64_photons": n,
             "events_per_path": r32[7]["stats"]["events"] / n32,
-            "fp32_vs_fp64_scaled_err": {"A": _scaled_err(a[:5], b[:5]), "Irt": _scaled_err(a[5], b[5]),
-                                        "Icb": _scaled_err(a[6], b[6])},
+            "fp32_vs_fp64": dict(_fp32_errs(res["fp32"], res["fp64"]), photons=n),
         }
     return out
 
@@ -360,6 +391,7 @@ def main():
     clocks = Clocks(local)
     barrier()
     kms, stats = [], []
+    raw = np.zeros(5 + 4 * cfg.Ntheta * cfg.Nphi + 5 * cfg.Nthetab * cfg.Nphib + 1)
     wall0 = time.perf_counter()
     for s in range(args.steps):
         flush.fill_(s & 0xFF)  # evict L2 between timed steps (outside the kernel's events)
@@ -368,6 +400,8 @@ def main():
         r = solve.read()
         kms.append(r["stats"]["kernel_ms"])
         stats.append(r["stats"])
+        raw += np.concatenate([r["A"], r["Irt"].ravel(), r["Icb"].ravel(), r["ladder"].ravel(),
+                               [r["stats"]["photons"]]])
     barrier()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
@@ -377,6 +411,15 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_dev = float(t.item())
     value = world * B * args.steps / t_dev
+    # The sharded form's one exchange: the ranks' raw tallies summed once, after the timed
+    # region (a single all-reduce of about 0.1 MB).
+    if dist:
+        t = torch.from_numpy(raw).to(f"cuda:{local}")
+        dist.all_reduce(t)
+        raw = t.cpu().numpy()
+    n_all = raw[-1]
+    tallies = {"ranks_summed": world, "photons": float(n_all), "energy_closure_err": float(abs(raw[:5].sum() / n_all - 1)),
+               "cb_peak_s11": float(raw[5 + 4 * cfg.Ntheta * cfg.Nphi] / n_all)}
 
     # ---- e2e: the drop-in call with host buffers (uploads, launch, copy back, free)
     e2e_times = []
@@ -440,15 +483,26 @@ def main():
         s32.launch(0, np64)
         r32 = s32.read()
         s32.close()
-        err32 = {k: _scaled_err(r32[k], r64[k]) for k in ("A", "Irt", "Icb", "ladder")}
+        err32 = dict(_fp32_errs(r32, r64), photons=np64)
+        # The plain per-ray FP64 kernel in two launches, both 256-thread blocks over a
+        # grid-stride loop: one thread per photon over the whole GPU (its best measured
+        # rate; more photons per thread measured slower: 3.3e3 paths/s at 2 and 3.1e3 at 4
+        # on 38 912 threads, against 4.6e3 at 1), and the reference's own launch,
+        # threads = min(maximum_threads = 8192, rays) (src/config.jl:69,
+        # src/MonteCarloRadiativeTransfer.jl:39,46), which fills 32 of the 152 SMs.
+        def plain_rate(threads, photons):
+            sp = M.Solve(cfg64.replace(number_of_rays=photons, maximum_threads=threads), g64, I0, ctx=ctx,
+                         precision="fp64", kernel="plain", seed=2)
+            sp.launch(0, photons)
+            rp = sp.read()
+            sp.close()
+            return photons / (rp["stats"]["kernel_ms"] / 1e3), rp["stats"]["blocks"]
+
         plain_threads = min(n64, 65536)
-        sp = M.Solve(cfg64.replace(maximum_threads=plain_threads), g64, I0, ctx=ctx, precision="fp64",
-                     kernel="plain", seed=2)
-        sp.launch(0, n64)
-        rp = sp.read()
-        sp.close()
+        vplain, plain_blocks = plain_rate(plain_threads, n64)
+        ref_threads, ref_ppt = 8192, 2
+        vplain_ref, ref_blocks = plain_rate(ref_threads, ref_threads * ref_ppt)
         v64 = np64 / (r64["stats"]["kernel_ms"] / 1e3)
-        vplain = n64 / (rp["stats"]["kernel_ms"] / 1e3)
         cpu_v, cores, cpu_dt = cpu_oracle_rate(args.cpu_sample)
         serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
         batch = batch_leg(M, ctx)
@@ -463,9 +517,17 @@ def main():
             "batch_uneven_slabs": batch,
             "fp64_persistent": {"value": v64, "unit": "paths/s", "sample_photons": np64},
             "fp64_plain": {"value": vplain, "unit": "paths/s", "sample_photons": n64,
-                           "threads": plain_threads},
-            "fp32_vs_fp64_scaled_err": err32,
+                           "threads": plain_threads, "blocks": plain_blocks, "block_size": 256,
+                           "photons_per_thread": n64 / plain_threads,
+                           "note": "the plain kernel's best measured rate (one photon per thread over the "
+                                   "whole GPU) is the denominator of fp32_over_fp64_plain"},
+            "fp64_plain_reference_launch": {"value": vplain_ref, "unit": "paths/s",
+                                            "sample_photons": ref_threads * ref_ppt, "threads": ref_threads,
+                                            "blocks": ref_blocks, "block_size": 256,
+                                            "photons_per_thread": ref_ppt},
+            "fp32_vs_fp64": err32,
             "fp32_over_fp64_plain": value / world / vplain,
+            "fp32_over_fp64_plain_reference_launch": value / world / vplain_ref,
             "fp32_over_fp64_persistent": value / world / v64,
             "cpu_baseline": {"value": cpu_v, "unit": "paths/s", "cores": cores, "kind": "port",
                              "sample": f"{args.cpu_sample} photons of the same workload, FP64, "
@@ -477,7 +539,8 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": B, "total_photons": TOTAL_PHOTONS,
+        "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": B,
+                   "photons_timed": world * B * args.steps, "full_workload_photons": FULL_WORKLOAD_PHOTONS,
                    "bins": {"Ntheta": cfg.Ntheta, "Nphi": cfg.Nphi, "Ntheta_b": cfg.Nthetab,
                             "Nphi_b": cfg.Nphib},
                    "mie_table_angles": 1801, "parallelism": f"photon shards x{world}",
@@ -485,6 +548,7 @@ def main():
                    "launch": {"block_size": stats[0]["block_size"], "blocks": stats[0]["blocks"]}},
         "e2e": e2e,
         "gpu_launches": args.steps,
+        "tallies": tallies,
         "wall_s_timed": wall,
         "cb_peak": {"mean_per_path": mu, "std_per_path": math.sqrt(var),
                     "paths_for_1pct_stderr": paths_1pct,

@@ -1445,6 +1445,9 @@ struct SrvReq {
   unsigned status = 0;
   double t_sub = 0, t_adm = 0, t_done = 0;
   std::vector<double> result;  // raw sums once done
+  double bins_per_event = 0;   // RT + CB bin evaluations of one event (CB weighted by its cost)
+  double cost = 0;             // estimated bin evaluations per photon (measured after each wave)
+  double meas[2] = {0, 0};     // photons and events finished so far (read back after a wave)
 };
 
 }  // namespace
@@ -1456,6 +1459,9 @@ struct mcrt_server {
   int bs = 256, blocks = 0, tf4 = 0;
   size_t smem = 0;
   cudaStream_t stream = nullptr;
+  // Read-backs after a wave (results, cost counters) run here, so that they do not queue
+  // behind the wave that waits on `stream`.
+  cudaStream_t copy_stream = nullptr;
   struct Slot {
     DevBuf d_wave, d_claim, d_status, d_state, d_tacc;
     DevInstance* h_wave = nullptr;  // pinned; read by the wave's copy when it runs
@@ -1487,6 +1493,26 @@ double request_footprint(const SrvReq& r) {
   for (int s = 0; s < r.D.n_scat; ++s)
     if (r.D.scat[s].kind == 1) b += 32.0 * (r.D.scat[s].ntheta + 1) + 4.0 * (r.D.scat[s].rp + 4);
   return b;
+}
+
+// Bin evaluations of one event: every RT bin (a slab event near both faces peels off into
+// both hemispheres) and every CB bin, a reciprocal-path CB bin counted as 3.2 RT bins (its
+// measured cost ratio in the transport kernel).
+double request_bins_per_event(const SrvReq& r) {
+  return (double)r.cfg.n_theta * r.cfg.n_phi + (r.cfg.compute_cb ? 3.2 * r.cfg.n_theta_b * r.cfg.n_phi_b : 0.0);
+}
+
+// Events per photon before any has been measured: the fewer of the events that
+// absorption alone takes to bring the weight to minimum_intensity and a diffusion
+// estimate (2 + tau^2 for the total optical size), capped by maximum_scattering_times.
+double request_events_prior(const SrvReq& r) {
+  double tau = 0.0, om = 0.0;
+  for (int i = 0; i < r.geom.n_layers; ++i) {
+    tau += r.layers[i].infinite ? 50.0 : r.layers[i].tau;
+    om = std::max(om, r.layers[i].omega);
+  }
+  const double absorb = std::log(1.0 / std::max(r.cfg.minimum_intensity, 1e-300)) / std::max(1.0 - om, 1e-4);
+  return std::max(1.0, std::min({(double)r.cfg.maximum_scattering_times, absorb, 2.0 + tau * tau}));
 }
 
 // Admits pending requests while the cap and slot count allow (under the lock).
@@ -1531,12 +1557,24 @@ int srv_retire(mcrt_server* S, int b) {
     r->status |= status;
     if (r->last_wave == sl.wave_id && r->next >= r->nph) finished.push_back(r);
   }
+  // The wave has finished (its event was waited on), so the finished requests' tallies
+  // are complete; the next wave, queued on S->stream, does not touch them.
   for (SrvReq* r : finished) {
     r->result.resize(r->per_inst);
     CK(cudaMemcpyAsync(r->result.data(), r->tally.p, r->per_inst * sizeof(double), cudaMemcpyDeviceToHost,
-                       S->stream));
+                       S->copy_stream));
   }
-  CK(cudaStreamSynchronize(S->stream));
+  // The photons and events each unfinished member has completed so far (a wave still
+  // running may be adding to them; the value is only an estimate): its measured cost per
+  // photon sizes its quanta in later waves.
+  if (S->o.wave_work >= 0)
+    for (SrvReq* r : sl.members)
+      if (!(r->last_wave == sl.wave_id && r->next >= r->nph))
+        CK(cudaMemcpyAsync(r->meas, r->D.acc + ACC_PHOTONS, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                           S->copy_stream));
+  CK(cudaStreamSynchronize(S->copy_stream));
+  for (SrvReq* r : sl.members)
+    if (r->meas[0] > 0) r->cost = r->bins_per_event * std::max(r->meas[1] / r->meas[0], 1.0);
   std::lock_guard<std::mutex> lk(S->mu);
   S->busy_s += ms * 1e-3;
   for (SrvReq* r : finished) {
@@ -1592,15 +1630,23 @@ int srv_build_wave(mcrt_server* S, int b, bool& launched) {
   if (members.empty()) return MCRT_OK;
   std::stable_sort(members.begin(), members.end(),
                    [](SrvReq* a, SrvReq* c) { return a->nph - a->next > c->nph - c->next; });
+  // Each member's quantum: with wave_work >= 0, its equal share of the wave's bin
+  // evaluations over its cost per photon, so that a costly request (long paths, many
+  // bins) does not lengthen the wave that cheap requests ride in; otherwise an equal
+  // share of wave_photons.
   const long long q = std::max<long long>(S->o.min_quantum, S->o.wave_photons / (long long)members.size());
+  const double share = S->o.wave_work / (double)members.size();
   const long long wid = S->next_wave++;
   for (int i = 0; i < S->o.max_active; ++i) {
     DevInstance& W = sl.h_wave[i];
     if (i < (int)members.size()) {
       SrvReq* r = members[i];
+      long long qi = q;
+      if (S->o.wave_work >= 0)
+        qi = std::max<long long>(32, (long long)std::min(share / std::max(r->cost, 1.0), 1e15));
       W = r->D;
       W.photon_begin = r->next;
-      W.n_photons = std::min<long long>(q, r->nph - r->next);
+      W.n_photons = std::min<long long>(qi, r->nph - r->next);
       r->next += W.n_photons;
       r->last_wave = wid;
       r->waves += 1;
@@ -1678,6 +1724,7 @@ extern "C" int mcrt_server_create(mcrt_ctx* ctx, const mcrt_server_opts* opts, m
   if (S->o.max_active <= 0) S->o.max_active = 256;
   if (S->o.wave_photons <= 0) S->o.wave_photons = 1 << 20;
   if (S->o.min_quantum <= 0) S->o.min_quantum = 4096;
+  if (S->o.wave_work == 0) S->o.wave_work = 8e9;
   if (S->o.precision != MCRT_FP32 && S->o.precision != MCRT_FP64)
     return set_err(MCRT_EINVAL, "precision must be MCRT_FP32 or MCRT_FP64");
   CK(cudaSetDevice(ctx->device));
@@ -1692,6 +1739,7 @@ extern "C" int mcrt_server_create(mcrt_ctx* ctx, const mcrt_server_opts* opts, m
   if (occ < 1) return set_err(MCRT_EINVAL, "server: kernel does not fit");
   S->blocks = ctx->sms * occ;
   CK(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking));
   const size_t slots = (size_t)S->blocks * S->bs;
   for (auto& sl : S->slot) {
     CK(sl.d_wave.alloc(S->o.max_active * sizeof(DevInstance)));
@@ -1772,6 +1820,8 @@ extern "C" int mcrt_server_submit(mcrt_server* S, const mcrt_request* q, uint64_
   r->footprint = request_footprint(*r);
   if (r->footprint > S->o.memory_cap_bytes)
     return set_err(MCRT_EBUSY, "request footprint exceeds the server's memory cap");
+  r->bins_per_event = request_bins_per_event(*r);
+  r->cost = r->bins_per_event * request_events_prior(*r);
   r->t_sub = now_s();
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->fatal) return set_err(S->fatal, "server stopped: " + S->fatal_msg);
@@ -1869,6 +1919,7 @@ extern "C" int mcrt_server_destroy(mcrt_server* S) {
     if (sl.done) cudaEventDestroy(sl.done);
   }
   cudaStreamDestroy(S->stream);
+  if (S->copy_stream) cudaStreamDestroy(S->copy_stream);
   delete S;
   return MCRT_OK;
 }

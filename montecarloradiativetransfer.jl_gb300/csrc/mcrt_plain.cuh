@@ -309,7 +309,10 @@ __global__ void __launch_bounds__(256) k_plain(PlainParams p) {
           for (int s = 0; s < 4; ++s) Eb[s] *= sc;
           T Eaf[4] = {Ea[0], Ea[1], Ea[2], Ea[3]};
           plain_update_E(s1, Eaf, kf0, kas);
-          const T raa = MT<T>::sqrt(Iaf[0] / (Eaf[0] * Eaf[0] + Eaf[1] * Eaf[1] + Eaf[2] * Eaf[2] + Eaf[3] * Eaf[3]));
+          // src/gpu.jl:84, with a slightly negative rounded intensity (90-degree Rayleigh
+          // scattering of a fully polarised photon) or a vanishing field clamped to zero.
+          const T nef = Eaf[0] * Eaf[0] + Eaf[1] * Eaf[1] + Eaf[2] * Eaf[2] + Eaf[3] * Eaf[3];
+          const T raa = nef > T(0) ? MT<T>::sqrt(fmax(Iaf[0], T(0)) / nef) : T(0);
           for (int s = 0; s < 4; ++s) {
             Ea[s] *= raa;
             Eb[s] *= raa;

@@ -498,7 +498,11 @@ __device__ int sample_event(PState<T>& ps, const DevInstance& in, const BinTable
     T Ef[4] = {ps.A[0], ps.A[1], ps.A[2], ps.A[3]};
     update_E(ks, Ef, kf0x, kf0y, kf0z, eh0x, eh0y, s1.kind, s1.S, s1.ntheta, table_scale<T>(s1));
     T nf = Ef[0] * Ef[0] + Ef[1] * Ef[1] + Ef[2] * Ef[2] + Ef[3] * Ef[3];
-    T c = MT<T>::sqrt(Iaf0[0] / nf);
+    // raa of src/gpu.jl:84. The backscattered intensity vanishes in exact arithmetic for a
+    // fully polarised photon scattered at 90 degrees by Rayleigh scatterers (P11 = -P12),
+    // where rounding can leave it slightly negative: clamped at zero (the reference's
+    // sqrt would throw there), as is a vanishing field norm.
+    T c = nf > T(0) ? MT<T>::sqrt(fmax(Iaf0[0], T(0)) / nf) : T(0);
     T rb = (T)MT<T>::expscale(ps.logL - ps.logA) * c;
     for (int s = 0; s < 4; ++s) {
       ev.ea[s] = ps.A[s] * c;

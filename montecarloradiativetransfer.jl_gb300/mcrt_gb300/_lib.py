@@ -77,7 +77,8 @@ class Stats(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("memory_cap_bytes", C.c_double), ("max_active", C.c_int), ("wave_photons", C.c_int64),
-                ("min_quantum", C.c_int64), ("precision", C.c_int), ("use_graphs", C.c_int)]
+                ("min_quantum", C.c_int64), ("precision", C.c_int), ("use_graphs", C.c_int),
+                ("wave_work", C.c_double)]
 
 
 class RequestC(C.Structure):

@@ -432,11 +432,11 @@ class Server:
 
     def __init__(self, *, ctx: Optional[Context] = None, memory_cap_bytes: float = 20e9, max_active: int = 256,
                  wave_photons: int = 1 << 20, min_quantum: int = 4096, precision: str = "fp32",
-                 use_graphs: bool = True, log_path: Optional[str] = None):
+                 use_graphs: bool = True, log_path: Optional[str] = None, wave_work: float = 0.0):
         self.ctx = ctx or default_context()
         self._log = open(log_path, "a", encoding="utf-8") if log_path else None
         o = _lib.ServerOpts(float(memory_cap_bytes), int(max_active), int(wave_photons), int(min_quantum),
-                            _PREC[precision], int(use_graphs))
+                            _PREC[precision], int(use_graphs), float(wave_work))
         h = C.c_void_p()
         check(lib().mcrt_server_create(self.ctx.h, C.byref(o), C.byref(h)))
         self.h = h

@@ -31,7 +31,11 @@
 //   * a rotated cosine that rounds below -1 is clamped instead of being read as the
 //     "sample a new angle" sentinel of phase_matrix (rayleigh.jl:9, mie.jl:47);
 //   * the unbounded loops (rejection loop cpu.jl:194-235, kepler_solver utils.jl:249)
-//     are capped; hitting a cap is counted and reported.
+//     are capped; hitting a cap is counted and reported;
+//   * the reciprocal-path amplitude scale raa = sqrt(Iaf / |Eaf|^2) (gpu.jl:84,
+//     cpu.jl:77) is taken as zero where the rounded backscattered intensity is negative
+//     or the field vanishes (a fully polarised photon scattered at 90 degrees by
+//     Rayleigh scatterers), where the reference's sqrt throws a DomainError.
 
 #include <algorithm>
 #include <cmath>
@@ -718,7 +722,11 @@ inline void collect_cb(const Ctx& C, Tally& T, V4 I, V3 k, V3 x, int idx, const 
     Eb2 *= sc;
     cplx Eaf1 = Ea1, Eaf2 = Ea2;
     update_E(sca, Eaf1, Eaf2, kf, kas);
-    double raa = std::sqrt(Iaf.v[0] / (std::norm(Eaf1) + std::norm(Eaf2)));
+    // gpu.jl:84; a rounded, slightly negative intensity (90-degree Rayleigh scattering of
+    // a fully polarised photon, P11 = -P12) or a vanishing field norm gives zero here,
+    // where the reference's sqrt would throw a DomainError.
+    const double nef = std::norm(Eaf1) + std::norm(Eaf2);
+    double raa = nef > 0 ? std::sqrt(std::max(Iaf.v[0], 0.0) / nef) : 0.0;
     Ea1 *= raa;
     Ea2 *= raa;
     Eb1 *= raa;
