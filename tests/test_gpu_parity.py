@@ -4,9 +4,9 @@ Tolerances (scaled errors as defined in helpers.scaled_err):
   * FP64 kernels vs the FP64 oracle on identical Philox streams: 1e-9 on every tally
     (both restate the same arithmetic; only rounding order differs).
   * FP32 persistent kernel vs its FP64 form on identical streams: 1e-4 on every tally.
-  * Independent streams: every Stokes element within 3 combined Monte Carlo standard
-    errors (batch means), allowing the 1% of elements that a 3-sigma band misses by
-    chance, and none beyond 5 sigma; the CB enhancement within 3 sigma.
+  * Independent streams: the oracle's per-element z against the GPU's batch means (mean
+    z^2 and max z per tally, and the CB enhancement) inside the distribution of the same
+    scores for 199 GPU estimates of equal size on independent photon ranges.
   * First scattering order vs the analytic single-scattering slab result: 1e-6 (FP64),
     1e-5 (FP32).
 """
@@ -15,7 +15,7 @@ import math
 import numpy as np
 import pytest
 
-from helpers import cb_peak_stats, reciprocity_z, scaled_err, sim_arrays
+from helpers import calibrated_independent_streams, cb_peak_stats, reciprocity_z, scaled_err, sim_arrays
 
 pytestmark = pytest.mark.gpu
 N0 = [1.0, 0.0, 0.0, 0.0]
@@ -125,28 +125,15 @@ def _batch_means(M, cfg, g, I0, prec, seed, nb):
 
 
 def test_statistics_agree_with_oracle_on_independent_streams(M, O, gpu_ctx):
+    """A small Rayleigh slab: the oracle on its own Philox streams against the GPU's batch
+    means, calibrated by 199 GPU estimates of the oracle's sample size
+    (helpers.calibrated_independent_streams)."""
     ray = M.RayleighScatterer(0.99, 100.0)
     g = M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=4 * ray.kl, scatterer=ray)])
     cfg = small_cfg(M, g, 2000)
-    nb = 16
-    R, C, L = _batch_means(M, cfg, g, N0, "fp32", 101, nb)
-    ref = O.simulate(cfg.replace(number_of_rays=4 * cfg.number_of_rays), g, N0, seed=202, threads=0)
-    nr = 4 * cfg.number_of_rays
-    gpu_mean = R.mean(0)
-    se_gpu = R.std(0, ddof=1) / math.sqrt(nb)
-    se_ref = R.std(0, ddof=1) * math.sqrt(cfg.number_of_rays / nr)  # same per-path variance
-    se = np.sqrt(se_gpu ** 2 + se_ref ** 2)
-    d = np.abs(gpu_mean - ref["Irt"] / nr)
-    mask = se > 0
-    z = d[mask] / se[mask]
-    assert np.mean(z > 3) < 0.01, np.mean(z > 3)
-    assert z.max() < 5.5, z.max()
-    # CB enhancement factor at exact backscatter: s11 of Icb over the ladder at theta_b = 0
-    enh = C[:, 0, 0, 0] / L[:, 0, 0]
-    enh_ref = ref["Icb"][0, 0, 0] / ref["ladder"][0, 0]
-    se_e = enh.std(ddof=1) / math.sqrt(nb) * math.sqrt(1 + cfg.number_of_rays * nb / nr)
-    assert abs(enh.mean() - enh_ref) < 3 * se_e, (enh.mean(), enh_ref, se_e)
-    assert 1.0 < enh_ref <= 2.0
+    pv = calibrated_independent_streams(M, O, cfg, g, N0, 2000, 8000, label="small rayleigh slab")
+    for k, p in pv.items():
+        assert p > 1.0 / 200, (k, p)
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-6), ("fp32", 1e-5)])

@@ -44,8 +44,10 @@ def _rank(rank, world, port, outdir, prec):
     count = N_PHOTONS - begin if rank == world - 1 else n
     s = M.Solve(cfg, g, [1, 0, 1, 0], precision=prec, seed=23)
     s.launch(begin, count)
-    flat = torch.from_numpy(_raw(s.read()).copy())
+    r = s.read()
     s.close()
+    np.save(os.path.join(outdir, f"rank{rank}_{prec}.npy"), np.array([begin, count, r["stats"]["photons"]]))
+    flat = torch.from_numpy(_raw(r).copy())
     dist.all_reduce(flat)
     if rank == 0:
         np.save(os.path.join(outdir, f"sharded_{prec}.npy"), flat.numpy())
@@ -60,6 +62,9 @@ def test_library_photon_shards_over_two_ranks_sum_to_one_run(M, O, gpu_ctx, tmp_
     port = 29700 + (os.getpid() % 1500) + (7 if prec == "fp32" else 0)
     mp.spawn(_rank, args=(2, port, str(tmp_path), prec), nprocs=2, join=True)
     sharded = np.load(tmp_path / f"sharded_{prec}.npy")
+    ranks = [np.load(tmp_path / f"rank{k}_{prec}.npy").tolist() for k in range(2)]
+    for begin, count, photons in ranks:  # each rank ran exactly its own range
+        assert photons == count, ranks
     cfg, g = _workload(M, O)
     s = M.Solve(cfg, g, [1, 0, 1, 0], precision=prec, seed=23)
     s.launch(0, N_PHOTONS)

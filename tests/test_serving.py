@@ -62,11 +62,18 @@ def test_server_results_match_simulate(M, gpu_ctx, mie5, mie2, tmp_path):
     assert len(lines) == len(reqs) and all(x["latency_s"] >= x["queued_s"] >= 0 for x in lines)
 
 
+@pytest.mark.parametrize("quanta", ["work", "photons"])
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
-def test_result_is_the_same_alone_and_in_the_mix(M, gpu_ctx, mie5, mie2, prec, tol):
+def test_result_is_the_same_alone_and_in_the_mix(M, gpu_ctx, mie5, mie2, prec, tol, quanta):
+    """Waves sized in bin evaluations (each request's quantum from its measured cost per
+    photon) and in photons: small waves, so that the request's photons are spread over
+    several waves shared with the others."""
     reqs = requests(M, mie5, mie2)
     x = reqs[4]
-    srv = M.Server(precision=prec, wave_photons=4096, min_quantum=512)
+    if quanta == "work":
+        srv = M.Server(precision=prec, wave_work=2e7)
+    else:
+        srv = M.Server(precision=prec, wave_photons=4096, min_quantum=512, wave_work=-1)
     c, g, I, n, s, i = x
     alone = srv.result(srv.submit(c, g, I, 4 * n, seed=s, instance=i))
     tickets = []
