@@ -1,7 +1,15 @@
 """Shared comparison helpers for the parity tests."""
 import math
+import socket
 
 import numpy as np
+
+
+def free_port() -> int:
+    """A TCP port on 127.0.0.1 that the OS reports free, for a process group's store."""
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
 
 
 def scaled_err(a, b):

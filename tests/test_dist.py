@@ -44,7 +44,9 @@ def _worker(rank, world, port, outdir):
 
 
 def test_photon_sharding_over_two_ranks_equals_one_run(tmp_path):
-    port = 29500 + (os.getpid() % 2000)
+    from helpers import free_port
+
+    port = free_port()
     mp.spawn(_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True)
     sharded = np.load(tmp_path / "sharded.npy")
     import oracle as O

@@ -59,7 +59,9 @@ def _rank(rank, world, port, outdir, prec):
 # batch depends on the launch, so the FP32 sums agree to the FP32 partials' rounding.
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-5)])
 def test_library_photon_shards_over_two_ranks_sum_to_one_run(M, O, gpu_ctx, tmp_path, prec, tol):
-    port = 29700 + (os.getpid() % 1500) + (7 if prec == "fp32" else 0)
+    from helpers import free_port
+
+    port = free_port()
     mp.spawn(_rank, args=(2, port, str(tmp_path), prec), nprocs=2, join=True)
     sharded = np.load(tmp_path / f"sharded_{prec}.npy")
     ranks = [np.load(tmp_path / f"rank{k}_{prec}.npy").tolist() for k in range(2)]
