@@ -12,8 +12,9 @@
 // tests derived from the reference's semantics: published Philox4x32-10 vectors,
 // exact per-photon energy closure, the analytic single-scattering slab reflection,
 // the Rayleigh sampler's density, an independent Mie evaluation, agreement of the
-// reference's O(n) reciprocal-path walk with the incremental form, and reciprocity of
-// the slab reflection function at the 3-sigma level.
+// reference's O(n) reciprocal-path walk with the incremental form, reciprocity of the
+// slab reflection function at the 3-sigma level, and agreement at all scattering orders
+// with an independently written analog polarised Monte Carlo on Rayleigh slabs.
 //
 // Random numbers: the reference calls an unseeded rand(). Here every draw comes from
 // Philox4x32-10 keyed by (seed, instance) with counter (photon, event, attempt), and

@@ -1,0 +1,125 @@
+"""An analog polarised Monte Carlo for a plane-parallel Rayleigh slab, written for the tests
+independently of the oracle and of the library.
+
+It follows photons the textbook way rather than the reference's way: no forced
+collisions, no peel-off and no weight renormalisation. A photon flies an exponential
+free path; if that takes it out of the slab it escapes and is counted in the direction
+it travels; otherwise it scatters. Scattering draws (Theta, phi) from the exact joint
+density of the polarised Rayleigh phase matrix, P11 I + P12 (Q cos 2phi + U sin 2phi),
+and keeps the photon's weight times the single-scattering albedo. The Stokes vector is
+carried in a local frame (e1, e2 = k x e1); Q = I_par - I_perp with respect to e1.
+
+Escaping photons give the reflected and transmitted fractions and their moments in the
+exit cosine, estimates of the same integrals that the oracle's peel-off tallies give by
+Gauss-Legendre quadrature, so the two can be compared at all scattering orders.
+"""
+import math
+
+import numpy as np
+
+
+def _rot(Q, U, phi):
+    """(Q, U) in a frame rotated by phi (from e1 towards e2)."""
+    c, s = np.cos(2 * phi), np.sin(2 * phi)
+    return Q * c + U * s, -Q * s + U * c
+
+
+def run(tau, omega, n, rng, max_orders=200, batches=20):
+    """Normal incidence from above (k0 = -z), unpolarised light, slab z in [-tau, 0].
+
+    Returns a dict of per-batch estimates (arrays of length `batches`) of:
+      R, T        reflected / diffusely transmitted fraction (scattered at least once),
+      R_mu, R_mu2 reflected moments E[w mu], E[w mu^2] (mu = exit cosine),
+      T_mu        transmitted moment,
+      R_Q         reflected Q in the exit meridian frame (e1 in the plane of z and k),
+      R1, R1_Q    the single-scattering part of R and R_Q."""
+    out = {k: np.zeros(batches) for k in ("R", "T", "R_mu", "R_mu2", "T_mu", "R_Q", "R1", "R1_Q")}
+    per = n // batches
+    for b in range(batches):
+        m = per
+        k = np.tile([0.0, 0.0, -1.0], (m, 1))
+        e1 = np.tile([1.0, 0.0, 0.0], (m, 1))
+        S = np.zeros((m, 4))
+        S[:, 0] = 1.0
+        z = np.zeros(m)
+        order = np.zeros(m, dtype=int)
+        alive = np.ones(m, dtype=bool)
+        for _ in range(max_orders + 1):
+            idx = np.nonzero(alive)[0]
+            if idx.size == 0:
+                break
+            t = rng.exponential(1.0, idx.size)
+            zn = z[idx] + t * k[idx, 2]
+            up = zn > 0.0
+            down = zn < -tau
+            for mask, key in ((up, "R"), (down, "T")):
+                j = idx[mask]
+                j = j[order[j] > 0]  # unscattered photons are the direct beam
+                if j.size == 0:
+                    continue
+                w = S[j, 0]
+                mu = np.abs(k[j, 2])
+                out[key][b] += w.sum()
+                out[key + "_mu"][b] += (w * mu).sum()
+                if key == "R":
+                    out["R_mu2"][b] += (w * mu * mu).sum()
+                    # Q in the exit meridian frame: e_par in the plane of z and k, normal to k
+                    zhat = np.array([0.0, 0.0, 1.0])
+                    ep = zhat[None, :] - k[j, 2:3] * k[j]
+                    ep /= np.linalg.norm(ep, axis=1)[:, None]
+                    e2 = np.cross(k[j], e1[j])
+                    chi = np.arctan2(np.einsum("ij,ij->i", ep, e2), np.einsum("ij,ij->i", ep, e1[j]))
+                    Qm, _ = _rot(S[j, 1], S[j, 2], chi)
+                    out["R_Q"][b] += Qm.sum()
+                    first = order[j] == 1
+                    out["R1"][b] += w[first].sum()
+                    out["R1_Q"][b] += Qm[first].sum()
+            alive[idx[up | down]] = False
+            stay = idx[~(up | down)]
+            if stay.size == 0:
+                break
+            z[stay] = zn[~(up | down)]
+            # the scattering angle from P11 = 3/4 (1 + c^2), by rejection
+            c = np.empty(stay.size)
+            todo = np.arange(stay.size)
+            while todo.size:
+                cc = rng.uniform(-1.0, 1.0, todo.size)
+                ok = rng.uniform(0.0, 2.0, todo.size) < 1.0 + cc * cc
+                c[todo[ok]] = cc[ok]
+                todo = todo[~ok]
+            p11 = 0.75 * (1 + c * c)
+            p12 = -0.75 * (1 - c * c)
+            I, Q, U, V = S[stay, 0], S[stay, 1], S[stay, 2], S[stay, 3]
+            # the azimuth of the scattering plane from the conditional density, by rejection
+            pol = np.sqrt(Q * Q + U * U) / I
+            bound = p11 + np.abs(p12) * pol
+            phi = np.empty(stay.size)
+            todo = np.arange(stay.size)
+            while todo.size:
+                ph = rng.uniform(0.0, 2 * math.pi, todo.size)
+                qr, _ = _rot(Q[todo], U[todo], ph)
+                dens = p11[todo] + p12[todo] * qr / I[todo]
+                ok = rng.uniform(0.0, 1.0, todo.size) * bound[todo] < dens
+                phi[todo[ok]] = ph[ok]
+                todo = todo[~ok]
+            Qr, Ur = _rot(Q, U, phi)
+            kk = k[stay]
+            e1o = e1[stay]
+            e2o = np.cross(kk, e1o)
+            e1p = np.cos(phi)[:, None] * e1o + np.sin(phi)[:, None] * e2o  # in the scattering plane
+            s = np.sqrt(np.maximum(1 - c * c, 0.0))
+            kn = c[:, None] * kk + s[:, None] * e1p
+            e1n = -s[:, None] * kk + c[:, None] * e1p
+            In = p11 * I + p12 * Qr
+            Qn = p12 * I + p11 * Qr
+            Un = 1.5 * c * Ur
+            Vn = 1.5 * c * V
+            scale = omega * I / In
+            S[stay] = np.stack([In, Qn, Un, Vn], axis=1) * scale[:, None]
+            k[stay] = kn / np.linalg.norm(kn, axis=1)[:, None]
+            e1[stay] = e1n / np.linalg.norm(e1n, axis=1)[:, None]
+            order[stay] += 1
+            alive[stay[order[stay] > max_orders]] = False
+        for key in out:
+            out[key][b] /= per
+    return out
