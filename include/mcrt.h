@@ -267,10 +267,11 @@ typedef struct {
   int64_t min_quantum;     /* at least this many photons per request per wave (0 = 4096) */
   int precision;           /* mcrt_precision */
   int use_graphs;          /* 0 = direct launches, 1 = replay captured CUDA graphs */
-  double wave_work;        /* bin evaluations per wave shared equally by the active requests;
-                            * each request's photon quantum is its share over its cost per
-                            * photon (estimated before its first wave, measured after each);
-                            * 0 = 8e9; < 0 sizes quanta in photons (wave_photons, min_quantum) */
+  double wave_work;        /* 0: photon quanta (above). > 0: bin evaluations per wave shared
+                            * equally by the active requests, each request's photon quantum
+                            * being its share over its cost per photon (estimated before its
+                            * first wave, measured after each); measured slower on the mixed
+                            * stream than photon quanta, kept as an option */
 } mcrt_server_opts;
 
 typedef struct {

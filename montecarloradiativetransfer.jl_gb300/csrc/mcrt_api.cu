@@ -1567,7 +1567,7 @@ int srv_retire(mcrt_server* S, int b) {
   // The photons and events each unfinished member has completed so far (a wave still
   // running may be adding to them; the value is only an estimate): its measured cost per
   // photon sizes its quanta in later waves.
-  if (S->o.wave_work >= 0)
+  if (S->o.wave_work > 0)
     for (SrvReq* r : sl.members)
       if (!(r->last_wave == sl.wave_id && r->next >= r->nph))
         CK(cudaMemcpyAsync(r->meas, r->D.acc + ACC_PHOTONS, 2 * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1630,10 +1630,10 @@ int srv_build_wave(mcrt_server* S, int b, bool& launched) {
   if (members.empty()) return MCRT_OK;
   std::stable_sort(members.begin(), members.end(),
                    [](SrvReq* a, SrvReq* c) { return a->nph - a->next > c->nph - c->next; });
-  // Each member's quantum: with wave_work >= 0, its equal share of the wave's bin
-  // evaluations over its cost per photon, so that a costly request (long paths, many
-  // bins) does not lengthen the wave that cheap requests ride in; otherwise an equal
-  // share of wave_photons.
+  // Each member's quantum: an equal share of wave_photons (at least min_quantum), or,
+  // with wave_work > 0, its equal share of the wave's bin evaluations over its cost per
+  // photon. The photon quanta measured better on the mixed request stream (lower median
+  // and tail latency, fewer GPU-busy seconds for the same work).
   const long long q = std::max<long long>(S->o.min_quantum, S->o.wave_photons / (long long)members.size());
   const double share = S->o.wave_work / (double)members.size();
   const long long wid = S->next_wave++;
@@ -1642,7 +1642,7 @@ int srv_build_wave(mcrt_server* S, int b, bool& launched) {
     if (i < (int)members.size()) {
       SrvReq* r = members[i];
       long long qi = q;
-      if (S->o.wave_work >= 0)
+      if (S->o.wave_work > 0)
         qi = std::max<long long>(32, (long long)std::min(share / std::max(r->cost, 1.0), 1e15));
       W = r->D;
       W.photon_begin = r->next;
@@ -1724,7 +1724,6 @@ extern "C" int mcrt_server_create(mcrt_ctx* ctx, const mcrt_server_opts* opts, m
   if (S->o.max_active <= 0) S->o.max_active = 256;
   if (S->o.wave_photons <= 0) S->o.wave_photons = 1 << 20;
   if (S->o.min_quantum <= 0) S->o.min_quantum = 4096;
-  if (S->o.wave_work == 0) S->o.wave_work = 8e9;
   if (S->o.precision != MCRT_FP32 && S->o.precision != MCRT_FP64)
     return set_err(MCRT_EINVAL, "precision must be MCRT_FP32 or MCRT_FP64");
   CK(cudaSetDevice(ctx->device));

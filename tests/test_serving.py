@@ -73,7 +73,7 @@ def test_result_is_the_same_alone_and_in_the_mix(M, gpu_ctx, mie5, mie2, prec, t
     if quanta == "work":
         srv = M.Server(precision=prec, wave_work=2e7)
     else:
-        srv = M.Server(precision=prec, wave_photons=4096, min_quantum=512, wave_work=-1)
+        srv = M.Server(precision=prec, wave_photons=4096, min_quantum=512)
     c, g, I, n, s, i = x
     alone = srv.result(srv.submit(c, g, I, 4 * n, seed=s, instance=i))
     tickets = []
