@@ -52,6 +52,17 @@ int set_err(int code, const std::string& msg) {
                      std::string(#call) + ": " + cudaGetErrorString(e_));                 \
   } while (0)
 
+// A host-to-device copy that has landed when it returns, ordered on `st`. A plain
+// cudaMemcpy from pageable memory may return before its DMA reaches the device, and it
+// runs on the legacy default stream, which a context's non-blocking stream does not wait
+// for: a later copy to the same buffer on that stream could then be overwritten by the
+// earlier one (seen as a solve's first launch running its creation-time photon range
+// while another process shared the GPU).
+inline cudaError_t upload_sync(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+}
+
 struct DevBuf {
   void* p = nullptr;
   size_t n = 0;
@@ -203,9 +214,9 @@ int mcrt_scatterer_create(mcrt_ctx* ctx, const mcrt_scatterer_desc* d, mcrt_scat
     CK(s->F.alloc(nf * sizeof(float4)));
     CK(s->S.alloc(nf * sizeof(float4)));
     CK(s->C.alloc(nc * sizeof(float)));
-    CK(cudaMemcpy(s->F.p, F.data(), nf * sizeof(float4), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->S.p, S.data(), nf * sizeof(float4), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->C.p, C.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
+    CK(upload_sync(s->F.p, F.data(), nf * sizeof(float4), ctx->stream));
+    CK(upload_sync(s->S.p, S.data(), nf * sizeof(float4), ctx->stream));
+    CK(upload_sync(s->C.p, C.data(), nc * sizeof(float), ctx->stream));
   }
   *out = s.release();
   return MCRT_OK;
@@ -496,7 +507,7 @@ struct Packer {
 };
 
 template <typename T>
-int upload_bins(const HostBins& H, DevBuf& buf) {
+int upload_bins(const HostBins& H, DevBuf& buf, cudaStream_t st) {
   Packer P;
   BinTables<T> hdr{};
   P.add(&hdr, sizeof(hdr));
@@ -546,7 +557,7 @@ int upload_bins(const HostBins& H, DevBuf& buf) {
   hdr.cpb = at(o_cpb);
   hdr.spb = at(o_spb);
   std::memcpy(P.bytes.data(), &hdr, sizeof(hdr));
-  CK(cudaMemcpy(buf.p, P.bytes.data(), P.bytes.size(), cudaMemcpyHostToDevice));
+  CK(upload_sync(buf.p, P.bytes.data(), P.bytes.size(), st));
   return MCRT_OK;
 }
 
@@ -781,7 +792,8 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
     if (it == bin_cache.end()) {
       HostBins H = make_bins(c, geoms[i]->kind, kfs[i]);
       std::unique_ptr<DevBuf> b(new DevBuf());
-      rc = G.L.precision == MCRT_FP32 ? upload_bins<float>(H, *b) : upload_bins<double>(H, *b);
+      rc = G.L.precision == MCRT_FP32 ? upload_bins<float>(H, *b, ctx->stream)
+                                      : upload_bins<double>(H, *b, ctx->stream);
       if (rc) return rc;
       bin_cache[key] = b->p;
       G.bins.push_back(std::move(b));
@@ -803,7 +815,7 @@ int build_group(mcrt_ctx* ctx, const mcrt_config* c, const mcrt_geometry* const*
   std::vector<DevInstance> dev(n);
   for (int s = 0; s < n; ++s) dev[s] = G.hinst[G.order[s]];
   CK(G.d_inst.alloc(n * sizeof(DevInstance)));
-  CK(cudaMemcpy(G.d_inst.p, dev.data(), n * sizeof(DevInstance), cudaMemcpyHostToDevice));
+  CK(upload_sync(G.d_inst.p, dev.data(), n * sizeof(DevInstance), ctx->stream));
   if (G.L.kernel == MCRT_KERNEL_PERSISTENT) {
     KInfo ki;
     kernel_info(G.L.precision, G.L.bs, ki);
