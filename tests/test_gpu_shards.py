@@ -74,3 +74,30 @@ def test_library_photon_shards_over_two_ranks_sum_to_one_run(M, O, gpu_ctx, tmp_
     s.close()
     assert whole[5:].any()
     assert np.max(np.abs(sharded - whole)) <= tol * np.max(np.abs(whole))
+
+
+def _first_launch(rank, prec, outdir):
+    import mcrt_gb300 as M
+    import oracle as O
+
+    cfg, g = _workload(M, O)
+    out = []
+    for trial in range(3):
+        s = M.Solve(cfg, g, [1, 0, 1, 0], precision=prec, seed=23 + trial)
+        begin = 3000 * rank
+        s.launch(begin, 3000)  # the first launch asks for a range other than the solve's own
+        out.append(s.read()["stats"]["photons"])
+        s.close()
+    np.save(os.path.join(outdir, f"first_{rank}_{prec}.npy"), np.array(out))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_first_launch_runs_its_range_while_another_process_shares_the_gpu(gpu_ctx, tmp_path, prec):
+    """Two processes create solves and launch at once on one GPU. Each solve's first launch
+    asks for a photon range other than the one the solve was created with; its instance
+    update must not be overtaken by the creation-time upload (a stale copy landing last
+    made such a launch run all 6 000 photons)."""
+    mp.spawn(_first_launch, args=(prec, str(tmp_path)), nprocs=2, join=True)
+    for rank in range(2):
+        got = np.load(tmp_path / f"first_{rank}_{prec}.npy")
+        assert np.all(got == 3000), (rank, got)
