@@ -26,6 +26,8 @@ src/cpu.jl:162-273, with the CB bin body of src/gpu.jl:41-175):
       199 GPU estimates of the same size on independent photon ranges (the docstring of
       helpers.calibrated_independent_streams says why a fixed per-element sigma rule is
       not valid here); also every batch finite and the CB enhancement factor in (1, 2].
+  (d) run_rt: the device Mueller assembly of all incident polarisation states against the
+      same assembly of the oracle's per-state results, 1e-9.
 
 The Mie tables come from the oracle's own bhmie and calculate_csrn (tests/conftest.py).
 """
@@ -122,3 +124,38 @@ def test_statistics_agree_with_the_oracle_on_independent_streams(M, O, gpu_ctx, 
     pv = calibrated_independent_streams(M, O, cfg, g, N0, n_b, n_ref, label=name)
     for k, p in pv.items():
         assert p > 1.0 / 200, (name, k, p)
+
+
+# photons per incident state for run_rt against the oracle (6 states on a slab, 2 on a sphere)
+RUN_RT_PHOTONS = {"rayleigh_slab": 48, "mie_slab": 256, "mie_sphere": 96}
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_run_rt_matches_the_oracle_at_the_benchmark_grids(M, O, gpu_ctx, mie5, mie2, name):
+    """run_rt (src/MonteCarloRadiativeTransfer.jl:87-291) as one batched FP64 launch with the
+    Mueller assembly on the device (mcrt_run_rt), against the same assembly (the numpy
+    restatement in helpers.assemble_run_rt) fed by the oracle's simulate of each incident
+    polarisation state on the same Philox streams (state i is instance i): every Mueller
+    element of the RT and CB tables and the energy budget at 1e-9 of their scale."""
+    from helpers import assemble_run_rt, table_of
+
+    n = RUN_RT_PHOTONS[name]
+    g, cfg = workload(M, name, mie5, mie2, n)
+    plane = g.kind == 0
+    sm_rt, sm_cb, energy, st = M.run_rt(cfg, g, seed=41, precision="fp64", with_stats=True)
+    assert st["status_flags"] & 5 == 0 and st["photons"] == n * (6 if plane else 2)
+
+    def sim(I, i):
+        r = O.simulate(cfg, g, I, seed=41, instance=i, threads=0)
+        return tuple(r["A"] / n) + (r["Irt"] / n, r["Icb"] / n)
+
+    MRT, MCB, G = assemble_run_rt(cfg, g, sim)
+    ref_rt, ref_cb = table_of(MRT, plane), table_of(MCB, plane)
+    scale_rt = max(np.max(np.abs(v)) for v in ref_rt.values())
+    scale_cb = max(np.max(np.abs(v)) for v in ref_cb.values())
+    for k in ref_rt:
+        assert np.max(np.abs(sm_rt[k] - ref_rt[k])) <= 1e-9 * scale_rt, (name, "RT", k)
+        assert np.max(np.abs(sm_cb[k] - ref_cb[k])) <= 1e-9 * scale_cb, (name, "CB", k)
+    E = [energy["direct_transmission"], energy["absorption"], energy["reflection"],
+         energy.get("transmission", 0.0), energy["remaining"]]
+    assert np.allclose(E, G, rtol=1e-9, atol=1e-15)
