@@ -8,7 +8,10 @@ it. Run ``python build.py`` from anywhere; ``__graft_entry__.build()`` calls
 from __future__ import annotations
 
 import concurrent.futures as cf
+import glob
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -44,8 +47,24 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("command failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
+def _fingerprint(nvcc: str, unit: str, extra: list[str]) -> str:
+    """Hash of everything an object depends on: the unit, every header beside it and in
+    include/, the host architecture, the compiler's path and the flags. An object whose
+    recorded fingerprint matches is reused."""
+    h = hashlib.sha256()
+    h.update(" ".join([platform.machine(), nvcc, *NVCC_FLAGS, *extra]).encode())
+    for path in [os.path.join(CSRC, unit)] + sorted(glob.glob(os.path.join(CSRC, "*.cuh")) +
+                                                    glob.glob(os.path.join(CSRC, "*.h")) +
+                                                    glob.glob(os.path.join(INCLUDE, "*.h"))):
+        h.update(path.encode())
+        with open(path, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
-    """Compiles every unit for sm_103a and links libmcrt.so; returns its path."""
+    """Compiles every unit for sm_103a (reusing objects whose sources, headers and flags
+    are unchanged) and links libmcrt.so; returns its path."""
     nvcc = _nvcc()
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
@@ -55,6 +74,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
 
     def compile_one(u: str) -> str:
         obj = os.path.join(OBJ_DIR, u.replace(".cu", ".o"))
+        stamp = obj + ".sha256"
+        fp = _fingerprint(nvcc, u, extra)
+        if not ptxas_info and os.path.exists(obj) and os.path.exists(stamp):
+            with open(stamp) as f:
+                if f.read().strip() == fp:
+                    return obj
         cmd = [nvcc, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, u), "-o", obj]
         if ptxas_info:
             r = subprocess.run(cmd, capture_output=True, text=True)
@@ -63,6 +88,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             sys.stderr.write(r.stderr)
         else:
             _run(cmd)
+        with open(stamp, "w") as f:
+            f.write(fp)
         return obj
 
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
