@@ -159,3 +159,48 @@ def test_run_rt_matches_the_oracle_at_the_benchmark_grids(M, O, gpu_ctx, mie5, m
     E = [energy["direct_transmission"], energy["absorption"], energy["reflection"],
          energy.get("transmission", 0.0), energy["remaining"]]
     assert np.allclose(E, G, rtol=1e-9, atol=1e-15)
+
+
+def more_geometry(M, name, mie5, mie2):
+    ray = M.RayleighScatterer(0.99, 100.0)
+    if name == "two_layers":
+        # Rayleigh over Mie: layer crossings, CB tied to layer 1. The upper layer is the
+        # thicker: moving up, the reference resets z to minus the thickness of the layer
+        # left (src/gpu.jl:238), which stays inside a thicker upper layer (a thinner one
+        # gives negative boundary distances, and NaN at the grid's horizontal CB bins,
+        # in the reference, the oracle and the kernels alike).
+        return M.PlaneGeometry(math.radians(160), 0.5, [M.Layer(d=2.0 * ray.kl, scatterer=ray),
+                                                        M.Layer(d=1.0 * mie5.kl, scatterer=mie5)]), [1, 0, 0, 1]
+    if name == "semi_infinite":  # a finite layer over a semi-infinite one
+        return M.PlaneGeometry(math.radians(140), 0.0, [M.Layer(d=0.5 * ray.kl, scatterer=ray),
+                                                        M.Layer(d=-1.0, scatterer=mie5, tau=math.inf)]), [1, 1, 0, 0]
+    if name == "sphere_circular":
+        return M.SphereGeometry(R=8.0 * mie2.kl, scatterer=mie2), [1, 0, 0, -1]
+    raise ValueError(name)
+
+
+@pytest.mark.parametrize("name", ["two_layers", "semi_infinite", "sphere_circular"])
+def test_fp64_and_fp32_on_more_geometries_at_default_grids(M, O, gpu_ctx, mie5, mie2, name):
+    """Geometries beside the benchmark configurations, at the reference's default grids
+    (Ntheta 64, Nphi 48, 51 CB angles, Nphi_b 8) and polarised incident light: the FP64
+    kernel against the oracle on identical streams (1e-9 of the scale, equal event
+    counts), and FP32 against FP64 (1e-4 of the scale)."""
+    g, I0 = more_geometry(M, name, mie5, mie2)
+    n = 256
+    cfg = M.Config(g, number_of_rays=n, maximum_scattering_times=2000)
+    ref = O.simulate(cfg, g, I0, seed=57, threads=0)
+    out = M.simulate(cfg, g, I0, precision="fp64", seed=57, with_extras=True)
+    A, Irt, Icb = sim_arrays(out)
+    st = out[7]["stats"]
+    assert st["status_flags"] & 5 == 0 and st["photons"] == n
+    assert st["events"] == ref["counters"]["events"]
+    for k, (a, b) in {"A": (A, ref["A"] / n), "Irt": (Irt, ref["Irt"] / n), "Icb": (Icb, ref["Icb"] / n),
+                      "ladder": (out[7]["ladder"], ref["ladder"] / n)}.items():
+        assert scaled_err(a, b) < 1e-9, (name, k, scaled_err(a, b))
+    n32 = 1 << 14
+    c32 = cfg.replace(number_of_rays=n32)
+    o64 = M.simulate(c32, g, I0, precision="fp64", seed=58, with_extras=True)
+    o32 = M.simulate(c32, g, I0, precision="fp32", seed=58, with_extras=True)
+    for i, k in ((5, "Irt"), (6, "Icb")):
+        assert scaled_err(o32[i], o64[i]) < 1e-4, (name, k, scaled_err(o32[i], o64[i]))
+    assert scaled_err(o32[7]["ladder"], o64[7]["ladder"]) < 1e-4
