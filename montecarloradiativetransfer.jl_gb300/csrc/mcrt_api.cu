@@ -428,6 +428,8 @@ struct HostBins {
   std::vector<int> upb;
   std::vector<double> stb, ctb, cpb, spb;
   int ntheta, nphi, nthetab, nphib, up0, up1, lo0, lo1;
+  std::vector<float> rtp;  // BinTables::rtp, 8 floats per pair
+  int rtp_lo = 0, rtp_zero = 0;
 };
 
 // Per-bin constants of the RT grid (config.jl:78-99) and of the CB grid rotated into
@@ -459,6 +461,28 @@ HostBins make_bins(const mcrt_config* c, int geom, const host::Sph& kfs) {
   for (int j = 0; j < c->n_phi; ++j) {
     H.cp.push_back(c->cos_phi[j]);
     H.sp.push_back(c->sin_phi[j]);
+  }
+  {
+    auto pairs = [&](int r0, int r1) {
+      const int np = (r1 - r0 + 1) / 2, npad = (np + RTP_PAD - 1) / RTP_PAD * RTP_PAD;
+      for (int p = 0; p < npad; ++p) {
+        const int ja = r0 + 2 * p, jb = ja + 1;
+        const bool oka = ja < r1, okb = jb < r1;
+        const int ia = oka ? ja : r0, ib = okb ? jb : r0;
+        const float v[8] = {(float)H.st[ia], (float)H.st[ib], (float)H.ct[ia], (float)H.ct[ib],
+                            (float)H.g[ia],  (float)H.g[ib],  oka ? (float)H.w[ia] : 0.f, okb ? (float)H.w[ib] : 0.f};
+        H.rtp.insert(H.rtp.end(), v, v + 8);
+      }
+    };
+    if (H.up1 > H.up0) pairs(H.up0, H.up1);
+    H.rtp_lo = (int)(H.rtp.size() / 8);
+    if (H.lo1 > H.lo0) pairs(H.lo0, H.lo1);
+    H.rtp_zero = (int)(H.rtp.size() / 8);
+    // lanes without bins evaluate a real bin at zero weight, so their arithmetic stays finite
+    const int i0 = H.up1 > H.up0 ? H.up0 : H.lo0;
+    const float z[8] = {(float)H.st[i0], (float)H.st[i0], (float)H.ct[i0], (float)H.ct[i0],
+                        (float)H.g[i0],  (float)H.g[i0],  0.f, 0.f};
+    for (int p = 0; p < RTP_PAD; ++p) H.rtp.insert(H.rtp.end(), z, z + 8);
   }
   for (int j = 0; j < c->n_theta_b; ++j) {
     H.stb.push_back(c->sin_theta_b[j]);
@@ -523,6 +547,7 @@ int upload_bins(const HostBins& H, DevBuf& buf, cudaStream_t st) {
          o_c1 = addv(H.c1), o_c2 = addv(H.c2), o_c3 = addv(H.c3);
   size_t o_upb = P.add(H.upb.data(), H.upb.size() * sizeof(int));
   size_t o_stb = addv(H.stb), o_ctb = addv(H.ctb), o_cpb = addv(H.cpb), o_spb = addv(H.spb);
+  size_t o_rtp = P.add(H.rtp.data(), H.rtp.size() * sizeof(float));
   CK(buf.alloc(P.bytes.size()));
   unsigned char* base = buf.as<unsigned char>();
   hdr.ntheta = H.ntheta;
@@ -556,6 +581,9 @@ int upload_bins(const HostBins& H, DevBuf& buf, cudaStream_t st) {
   hdr.ctb = at(o_ctb);
   hdr.cpb = at(o_cpb);
   hdr.spb = at(o_spb);
+  hdr.rtp = reinterpret_cast<const float4*>(base + o_rtp);
+  hdr.rtp_lo = H.rtp_lo;
+  hdr.rtp_zero = H.rtp_zero;
   std::memcpy(P.bytes.data(), &hdr, sizeof(hdr));
   CK(upload_sync(buf.p, P.bytes.data(), P.bytes.size(), st));
   return MCRT_OK;
@@ -2006,6 +2034,7 @@ std::vector<unsigned char> pack_bins_at(const HostBins& H, const unsigned char* 
          o_c1 = addv(H.c1), o_c2 = addv(H.c2), o_c3 = addv(H.c3);
   size_t o_upb = P.add(H.upb.data(), H.upb.size() * sizeof(int));
   size_t o_stb = addv(H.stb), o_ctb = addv(H.ctb), o_cpb = addv(H.cpb), o_spb = addv(H.spb);
+  size_t o_rtp = P.add(H.rtp.data(), H.rtp.size() * sizeof(float));
   hdr.ntheta = H.ntheta;
   hdr.nphi = H.nphi;
   hdr.nthetab = H.nthetab;
@@ -2037,6 +2066,9 @@ std::vector<unsigned char> pack_bins_at(const HostBins& H, const unsigned char* 
   hdr.ctb = at(o_ctb);
   hdr.cpb = at(o_cpb);
   hdr.spb = at(o_spb);
+  hdr.rtp = reinterpret_cast<const float4*>(dev + o_rtp);
+  hdr.rtp_lo = H.rtp_lo;
+  hdr.rtp_zero = H.rtp_zero;
   std::memcpy(P.bytes.data(), &hdr, sizeof(hdr));
   return P.bytes;
 }

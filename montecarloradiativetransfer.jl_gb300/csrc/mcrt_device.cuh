@@ -106,7 +106,15 @@ struct BinTables {
   const int* upb;
   // CB grid itself: per theta_b index sin, cos; per phi_b index cos, sin.
   const T *stb, *ctb, *cpb, *spb;
+  // RT polar bins in pairs for the packed FP32 tiles, read per event through L1 rather
+  // than held in registers: per pair {st0, st1, ct0, ct1}, {g0, g1, w0, w1}. The upper
+  // then the lower hemisphere, each padded with zero-weight pairs to a multiple of
+  // RTP_PAD pairs, then RTP_PAD zero-weight pairs for lanes without bins.
+  const float4* rtp;
+  int rtp_lo;    // first pair of the lower hemisphere
+  int rtp_zero;  // first of the trailing zero-weight pairs
 };
+constexpr int RTP_PAD = 4;  // a multiple of every tile's pairs per lane (2 or 4)
 
 // ------------------------------------------------------------------ Philox4x32-10
 // Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11.

@@ -876,7 +876,7 @@ __device__ __forceinline__ P2 acos2_scaled(P2 x, float scale) {
 
 template <int NP>
 struct RTLaneF2 {
-  P2 st[NP], ct[NP], g[NP], w[NP];
+  const float4* pc;  // this lane's first pair of polar-bin constants (BinTables::rtp)
   float cb, sb;
   P2 acc[NP][4];
 };
@@ -900,9 +900,13 @@ __device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float
   P2 esc = p2s(0.f);
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
-    const P2 k1 = fma2(R.st[i], A1, R.ct[i] * NFST);
-    const P2 k2 = R.st[i] * SD;
-    const P2 k3 = fma2(R.st[i], A3, R.ct[i] * FCT);
+    // the pair's polar constants come through L1 each event, which frees the registers
+    // that holding them would take (fewer spills at the 128-register cap)
+    const float4 pa = R.pc[2 * i], pb = R.pc[2 * i + 1];
+    const P2 Rst = p2(pa.x, pa.y), Rct = p2(pa.z, pa.w), Rg = p2(pb.x, pb.y), Rw = p2(pb.z, pb.w);
+    const P2 k1 = fma2(Rst, A1, Rct * NFST);
+    const P2 k2 = Rst * SD;
+    const P2 k3 = fma2(Rst, A3, Rct * FCT);
     P2 s2 = fma2(k1, k1, k2 * k2);
     // An RT bin exactly along the photon direction has probability zero; the clamp only
     // keeps the arithmetic finite there.
@@ -949,14 +953,14 @@ __device__ __forceinline__ float rt_event_f2(RTLaneF2<NP>& R, const EventP<float
     const P2 r2 = fma2(c2p, o2, (s2p * o1) * M1);
     P2 t2;
     if (SPHERE) {
-      const P2 kx = fma2(R.st[i], QX, R.ct[i] * XZ);
+      const P2 kx = fma2(Rst, QX, Rct * XZ);
       t2 = p2(sphere_t(kx.v.x, E.Da), sphere_t(kx.v.y, E.Da)) * p2s((float)LOG2E_D);
     } else {
-      t2 = A * R.g[i];
+      t2 = A * Rg;
     }
     const P2 ex = p2(t2.v.x <= tau0l ? MT<float>::exp2n(t2.v.x) : 0.f,
                      t2.v.y <= tau0l ? MT<float>::exp2n(t2.v.y) : 0.f);
-    const P2 wgt = ex * R.w[i];
+    const P2 wgt = ex * Rw;
     R.acc[i][0] = fma2(o0, wgt, R.acc[i][0]);
     R.acc[i][1] = fma2(r1, wgt, R.acc[i][1]);
     R.acc[i][2] = fma2(r2, wgt, R.acc[i][2]);
@@ -971,6 +975,7 @@ __device__ void rt_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
                            int q0, int q1) {
   static_assert(NB % 2 == 0, "bins are paired");
   constexpr int NP = NB / 2;
+  static_assert(RTP_PAD % NP == 0, "a lane's pairs lie within a hemisphere's padded pairs");
   const int lane = threadIdx.x & 31;
   const int r0 = upper ? B.up0 : B.lo0, r1 = upper ? B.up1 : B.lo1;
   const int ngrp = (r1 - r0 + NB - 1) / NB;
@@ -981,26 +986,11 @@ __device__ void rt_tile_f2(Shared<float, BS>& sh, const BinTables<float>& B, int
   RTLaneF2<NP> R;
   R.cb = B.cp[j2];
   R.sb = B.sp[j2];
-  float st[NB], ct[NB], g[NB], w[NB];
+  R.pc = B.rtp + 2 * (lane_ok ? (upper ? 0 : B.rtp_lo) + grp * NP : B.rtp_zero);
 #pragma unroll
-  for (int i = 0; i < NB; ++i) {
-    int j1 = r0 + grp * NB + i;
-    bool ok = lane_ok && j1 < r1;
-    int jj = ok ? j1 : r0;
-    st[i] = B.st[jj];
-    ct[i] = B.ct[jj];
-    g[i] = B.g[jj];
-    w[i] = ok ? B.w[jj] : 0.f;
-  }
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    R.st[i] = p2(st[2 * i], st[2 * i + 1]);
-    R.ct[i] = p2(ct[2 * i], ct[2 * i + 1]);
-    R.g[i] = p2(g[2 * i], g[2 * i + 1]);
-    R.w[i] = p2(w[2 * i], w[2 * i + 1]);
+  for (int i = 0; i < NP; ++i)
 #pragma unroll
     for (int s = 0; s < 4; ++s) R.acc[i][s] = p2s(0.f);
-  }
   const DevInstance& in = sh.inst;
   const float tau0l = (float)(in.tau0 * LOG2E_D);
   const int li = upper ? 0 : 1;
