@@ -44,11 +44,11 @@ FLOPS_RT_MIE = 128.349
 FLOPS_CBN_MIE = 409.0
 FLOPS_CB1_MIE = 196.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one transport launch
-# per photon, from an ncu capture of `bench.py --case 524288` (25.3 MB read + 5.97 GB
-# written for 524 288 photons). The traffic is
-# the per-event photon-state pool and scales with the photons, so a full launch is this
-# times its photons.
-NCU_DRAM_BYTES_PER_PHOTON = 11433.0
+# per photon, from an ncu capture of `bench.py --case 524288` (3.77 MB read + 1.214 GB
+# written for 524 288 photons). The traffic is dirty L2 lines of the per-event
+# photon-state pool and of the threads' spill slots written back; it scales with the
+# photons' events, so a full launch is this times its photons.
+NCU_DRAM_BYTES_PER_PHOTON = 2321.9
 
 
 def parse():
