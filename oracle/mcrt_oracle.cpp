@@ -14,7 +14,8 @@
 // the Rayleigh sampler's density, an independent Mie evaluation, agreement of the
 // reference's O(n) reciprocal-path walk with the incremental form, reciprocity of the
 // slab reflection function at the 3-sigma level, and agreement at all scattering orders
-// with an independently written analog polarised Monte Carlo on Rayleigh slabs.
+// with an independently written analog polarised Monte Carlo on Rayleigh slabs and on a
+// slab of absorbing Mie spheres.
 //
 // Random numbers: the reference calls an unseeded rand(). Here every draw comes from
 // Philox4x32-10 keyed by (seed, instance) with counter (photon, event, attempt), and

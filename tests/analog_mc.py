@@ -1,12 +1,15 @@
-"""An analog polarised Monte Carlo for a plane-parallel Rayleigh slab, written for the tests
-independently of the oracle and of the library.
+"""An analog polarised Monte Carlo for a plane-parallel slab of Rayleigh scatterers or of
+spheres with a tabulated phase matrix, written for the tests independently of the oracle
+and of the library.
 
 It follows photons the textbook way rather than the reference's way: no forced
 collisions, no peel-off and no weight renormalisation. A photon flies an exponential
 free path; if that takes it out of the slab it escapes and is counted in the direction
 it travels; otherwise it scatters. Scattering draws (Theta, phi) from the exact joint
-density of the polarised Rayleigh phase matrix, P11 I + P12 (Q cos 2phi + U sin 2phi),
-and keeps the photon's weight times the single-scattering albedo. The Stokes vector is
+density of the phase matrix, P11 I + P12 (Q cos 2phi + U sin 2phi), and keeps the
+photon's weight times the single-scattering albedo. For Rayleigh scatterers the matrix is
+analytic; for spheres it is tabulated (TabulatedPhase) and Theta is drawn by inverting the
+CDF of the tabulated P11, integrated on a fine grid. The Stokes vector is
 carried in a local frame (e1, e2 = k x e1); Q = I_par - I_perp with respect to e1.
 
 Escaping photons give the reflected and transmitted fractions and their moments in the
@@ -24,8 +27,30 @@ def _rot(Q, U, phi):
     return Q * c + U * s, -Q * s + U * c
 
 
-def run(tau, omega, n, rng, max_orders=200, batches=20):
+class TabulatedPhase:
+    """The phase matrix of spheres tabulated on uniform scattering angles over [0, pi]: P11,
+    P12, P33, P34, linear in the angle between nodes. The Mueller matrix in the scattering
+    plane is [[P11, P12, 0, 0], [P12, P11, 0, 0], [0, 0, P33, P34], [0, 0, -P34, P33]]."""
+
+    def __init__(self, F11, F12, F33, F34, fine=400001):
+        self.F = [np.asarray(f, float) for f in (F11, F12, F33, F34)]
+        self.theta = np.linspace(0.0, math.pi, len(self.F[0]))
+        th = np.linspace(0.0, math.pi, fine)
+        pdf = np.interp(th, self.theta, self.F[0]) * np.sin(th)
+        cdf = np.concatenate([[0.0], np.cumsum(0.5 * (pdf[1:] + pdf[:-1]) * np.diff(th))])
+        self._cdf, self._th = cdf / cdf[-1], th
+
+    def sample_cos(self, u):
+        return np.cos(np.interp(u, self._cdf, self._th))
+
+    def elements(self, c):
+        th = np.arccos(np.clip(c, -1.0, 1.0))
+        return [np.interp(th, self.theta, f) for f in self.F]
+
+
+def run(tau, omega, n, rng, max_orders=200, batches=20, phase=None):
     """Normal incidence from above (k0 = -z), unpolarised light, slab z in [-tau, 0].
+    `phase` is None for Rayleigh scatterers, else a TabulatedPhase.
 
     Returns a dict of per-batch estimates (arrays of length `batches`) of:
       R, T        reflected / diffusely transmitted fraction (scattered at least once),
@@ -79,16 +104,22 @@ def run(tau, omega, n, rng, max_orders=200, batches=20):
             if stay.size == 0:
                 break
             z[stay] = zn[~(up | down)]
-            # the scattering angle from P11 = 3/4 (1 + c^2), by rejection
-            c = np.empty(stay.size)
-            todo = np.arange(stay.size)
-            while todo.size:
-                cc = rng.uniform(-1.0, 1.0, todo.size)
-                ok = rng.uniform(0.0, 2.0, todo.size) < 1.0 + cc * cc
-                c[todo[ok]] = cc[ok]
-                todo = todo[~ok]
-            p11 = 0.75 * (1 + c * c)
-            p12 = -0.75 * (1 - c * c)
+            if phase is None:
+                # the scattering angle from P11 = 3/4 (1 + c^2), by rejection
+                c = np.empty(stay.size)
+                todo = np.arange(stay.size)
+                while todo.size:
+                    cc = rng.uniform(-1.0, 1.0, todo.size)
+                    ok = rng.uniform(0.0, 2.0, todo.size) < 1.0 + cc * cc
+                    c[todo[ok]] = cc[ok]
+                    todo = todo[~ok]
+                p11 = 0.75 * (1 + c * c)
+                p12 = -0.75 * (1 - c * c)
+                p33 = 1.5 * c
+                p34 = np.zeros_like(c)
+            else:
+                c = phase.sample_cos(rng.uniform(0.0, 1.0, stay.size))
+                p11, p12, p33, p34 = phase.elements(c)
             I, Q, U, V = S[stay, 0], S[stay, 1], S[stay, 2], S[stay, 3]
             # the azimuth of the scattering plane from the conditional density, by rejection
             pol = np.sqrt(Q * Q + U * U) / I
@@ -112,8 +143,8 @@ def run(tau, omega, n, rng, max_orders=200, batches=20):
             e1n = -s[:, None] * kk + c[:, None] * e1p
             In = p11 * I + p12 * Qr
             Qn = p12 * I + p11 * Qr
-            Un = 1.5 * c * Ur
-            Vn = 1.5 * c * V
+            Un = p33 * Ur + p34 * V
+            Vn = -p34 * Ur + p33 * V
             scale = omega * I / In
             S[stay] = np.stack([In, Qn, Un, Vn], axis=1) * scale[:, None]
             k[stay] = kn / np.linalg.norm(kn, axis=1)[:, None]

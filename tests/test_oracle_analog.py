@@ -1,7 +1,8 @@
 """An independent multiple-scattering anchor for the oracle: the oracle (forced collisions,
 peel-off into Gauss-Legendre bins, weight renormalised by the escape estimate, as the
 reference's cpu.jl/gpu.jl do) against an analog polarised Monte Carlo written apart from
-it (tests/analog_mc.py: free flights, escape counting, exact polarised Rayleigh sampling).
+it (tests/analog_mc.py: free flights, escape counting, exact sampling of the polarised
+phase matrix), on Rayleigh slabs and on a slab of absorbing Mie spheres.
 
 Both estimate the same integrals of the escaping light at all scattering orders: the
 reflected and diffusely transmitted fractions, their first moments in the exit cosine,
@@ -39,18 +40,37 @@ def _oracle(O, g, n, nb, max_scat=10000):
     return {k: np.array(v) for k, v in res.items()}
 
 
-@pytest.mark.parametrize("tau,omega,n_analog,n_oracle", [(1.0, 0.95, 1_000_000, 20000), (3.0, 0.99, 1_000_000, 10000)])
-def test_oracle_agrees_with_an_analog_polarised_monte_carlo(O, tau, omega, n_analog, n_oracle):
-    ray = O.RayleighScatterer(omega, 1.0)
-    g = O.PlaneGeometry(math.pi, 0.0, [O.Layer(d=tau, scatterer=ray)])
-    a = analog_mc.run(tau, omega, n_analog, np.random.default_rng(5), batches=20)
+def _compare(O, g, a, n_oracle, label):
     o = _oracle(O, g, n_oracle, 10)
     for k in QUANTITIES:
         ma, sa = a[k].mean(), a[k].std(ddof=1) / math.sqrt(len(a[k]))
         mo, so = o[k].mean(), o[k].std(ddof=1) / math.sqrt(len(o[k]))
         z = (ma - mo) / math.hypot(sa, so)
-        print(f"tau {tau} {k}: analog {ma:.5f} +- {sa:.5f}, oracle {mo:.5f} +- {so:.5f}, z {z:.2f}")
+        print(f"{label} {k}: analog {ma:.5f} +- {sa:.5f}, oracle {mo:.5f} +- {so:.5f}, z {z:.2f}")
         assert abs(z) < 4.0, (k, ma, mo, z)
     o1 = _oracle(O, g, 8000, 4, max_scat=1)
     for ka, ko in (("R1", "R"), ("R1_Q", "R_Q")):
+        print(f"{label} {ka}: analog {a[ka].mean():.5f}, oracle {o1[ko].mean():.5f}")
         assert abs(a[ka].mean() / o1[ko].mean() - 1) < 0.02, (ka, a[ka].mean(), o1[ko].mean())
+
+
+@pytest.mark.parametrize("tau,omega,n_analog,n_oracle", [(1.0, 0.95, 1_000_000, 20000), (3.0, 0.99, 1_000_000, 10000)])
+def test_oracle_agrees_with_an_analog_polarised_monte_carlo(O, tau, omega, n_analog, n_oracle):
+    ray = O.RayleighScatterer(omega, 1.0)
+    g = O.PlaneGeometry(math.pi, 0.0, [O.Layer(d=tau, scatterer=ray)])
+    a = analog_mc.run(tau, omega, n_analog, np.random.default_rng(5), batches=20)
+    _compare(O, g, a, n_oracle, f"rayleigh tau {tau}")
+
+
+def test_oracle_agrees_with_an_analog_monte_carlo_on_a_mie_slab(O):
+    """Spheres x = 2, m = 1.5+0.01i (omega 0.951, asymmetry 0.63) in a slab of tau = 1. This
+    exercises the oracle's Mie path: Theta drawn from calculate_csrn's inverse CDF
+    (utils.jl:263-287), the Kepler azimuth, and the interpolated phase matrix in update_I
+    (mie.jl:46-74). The analog run uses the same tables, which test_oracle.py pins to an
+    independent Mie evaluation, but none of the oracle's sampling or transport."""
+    tau = 1.0
+    mie = O.MieScatterer(2.0 / (2 * math.pi), 1.5 + 0.01j, 1.0, 0.1, Ntheta=1801)
+    g = O.PlaneGeometry(math.pi, 0.0, [O.Layer(d=tau * mie.kl, scatterer=mie)])
+    phase = analog_mc.TabulatedPhase(mie.F11, mie.F12, mie.F33, mie.F34)
+    a = analog_mc.run(tau, mie.omega, 1_000_000, np.random.default_rng(6), batches=20, phase=phase)
+    _compare(O, g, a, 20000, "mie x=2 tau 1")
