@@ -13,9 +13,12 @@
 // exact per-photon energy closure, the analytic single-scattering slab reflection,
 // the Rayleigh sampler's density, an independent Mie evaluation, agreement of the
 // reference's O(n) reciprocal-path walk with the incremental form, reciprocity of the
-// slab reflection function at the 3-sigma level, and agreement at all scattering orders
+// slab reflection function at the 3-sigma level, agreement at all scattering orders
 // with an independently written analog polarised Monte Carlo on Rayleigh slabs and on a
-// slab of absorbing Mie spheres.
+// slab of absorbing Mie spheres, and agreement at all orders with an exact vector
+// adding-doubling solution (tests/doubling.py): every RT bin's full Stokes vector for
+// four incident polarisation states, and the CB ladder, CB intensity and enhancement
+// factor at exact backscatter, where reciprocity fixes the interference term.
 //
 // Random numbers: the reference calls an unseeded rand(). Here every draw comes from
 // Philox4x32-10 keyed by (seed, instance) with counter (photon, event, attempt), and

@@ -1,0 +1,216 @@
+"""The oracle against an exact deterministic solution at every bin and every order: the
+vector adding-doubling solver of tests/doubling.py (Hansen & Travis 1974; de Haan, Bosma
+& Hovenier 1987), written apart from the oracle, gives the reflection and diffuse
+transmission matrices of a homogeneous slab to quadrature accuracy.
+
+The oracle's RT tally of a run with incident Stokes vector I0 estimates, per bin,
+Irt[:, j, k] / n = 4 |mu_j| inorm_j D R(mu_j, mu0, phi_k - phi0) D I0 (T in place of R
+for the lower hemisphere), where R is in the normalisation of those papers and
+D = diag(1, 1, -1, -1): the oracle takes Stokes vectors in the frame (e_theta, -e_phi)
+(the reference's get_basis, src/utils.jl:52-62, gives Eh = (sin phi, -cos phi, 0)),
+which is left-handed about the direction of travel, so its U and V are the negatives
+of the right-handed meridian frame's. The first-order test fixes D, with the oracle's
+exact single-scattering mode (one order, first-collision depth on a midpoint grid);
+the all-orders test then runs the four incident states [1,0,0,0], [1,1,0,0], [1,0,1,0],
+[1,0,0,1], which give all 16 elements of the matrices, and scores every bin of both
+hemispheres against the exact values with standard errors from batch means.
+
+This pins what the analog Monte Carlo of tests/analog_mc.py does not: the angular
+distribution and the polarisation of every Mueller element at multiple orders, for
+oblique incidence, in Rayleigh and in Mie slabs, through the reference's own scheme
+(forced collisions, peel-off into the Gauss-Legendre bins, weights lowered by the
+bin-quadrature escape estimate of src/gpu.jl:285-294; at the reference's default 64 x 48
+grid that estimate's error stays below the noise here).
+
+The same runs pin the coherent-backscattering tallies at exact backscatter, where
+reciprocity fixes the interference of reciprocal paths as a linear function of the
+exact ladder matrix (doubling.cyclical): the ladder, the CB intensity and the CB
+enhancement factor for each incident state."""
+import math
+
+import numpy as np
+import pytest
+
+import doubling as D
+
+STATES = np.array([[1.0, 0, 0, 0], [1, 1, 0, 0], [1, 0, 1, 0], [1, 0, 0, 1]])
+FRAME = np.diag([1.0, 1.0, -1.0, -1.0])
+THETA0 = math.radians(150.0)  # 30 degrees from the normal, travelling downwards
+TAU = 1.0
+
+
+def _case(O, kind):
+    if kind == "rayleigh":
+        s = O.RayleighScatterer(0.9, 1.0)
+        return s, D.rayleigh_matrix, 2, 16
+    s = O.MieScatterer(2.0 / (2 * math.pi), 1.5 + 0.01j, 1.0, 0.1, Ntheta=1801)  # omega 0.951, g 0.63
+    t = s.rounded_fp32()  # the oracle interpolates the FP32-rounded tables, as the device does
+    return s, D.TabulatedMatrix(t.F11, t.F12, t.F33, t.F34), 24, 128
+
+
+def _expected(sol, cfg, mu0):
+    """4 |mu| inorm D R D I0 per incident state, Stokes parameter and bin."""
+    phi = np.arctan2(cfg.sinphi, cfg.cosphi)
+    out = np.zeros((4, 4, cfg.Ntheta, cfg.Nphi))
+    for j, mu in enumerate(cfg.costheta):
+        M = sol.reflection(mu, mu0, phi) if mu > 0 else sol.transmission(-mu, mu0, phi)
+        M = FRAME @ M @ FRAME * (4 * abs(mu) * cfg.inorm[j])  # (Nphi, 4, 4)
+        out[:, :, j, :] = np.einsum("kab,sb->sak", M, STATES)
+    return out
+
+
+def _solve(O, kind, cfg, n_doublings=30):
+    s, F, n_modes, n_az = _case(O, kind)
+    h = cfg.Ntheta // 2
+    mu0 = abs(math.cos(THETA0))
+    q, w = D.half_range_gauss(h)  # the bins' own half-range Gauss-Legendre nodes
+    sol = D.solve(TAU, s.omega, F, q, w, extra_mu=[mu0], n_modes=n_modes, n_azimuth=n_az,
+                  n_doublings=n_doublings)
+    assert sol.dropped_mode_norm < 1e-6  # the azimuthal modes left out are negligible
+    return sol, mu0
+
+
+def _geometry(O, s):
+    return O.PlaneGeometry(THETA0, 0.0, [O.Layer(d=TAU * s.kl, scatterer=s)])
+
+
+def test_doubling_solver_conserves_energy_and_obeys_reciprocity(O):
+    """The solver's own checks: at omega = 1 reflected + diffusely transmitted + direct
+    flux is 1 for every incidence node; Rayleigh phase matrices have no azimuthal modes
+    beyond 2; and for a Mie phase matrix, at all orders, the reciprocity relation
+    R(mu_a, mu_b, dphi) = Q R(mu_b, mu_a, dphi)^T Q with Q = diag(1, 1, 1, -1) and the
+    mirror relation R(mu, mu0, -dphi) = P R(mu, mu0, dphi) P with P = diag(1, 1, -1, -1)
+    (Hovenier, van der Mee & Domke, Transfer of Polarized Light, 2004, sec. 5.3; the
+    signs are those of a right-handed meridian frame)."""
+    q, w = D.half_range_gauss(16)
+    sol = D.solve(1.0, 1.0, D.rayleigh_matrix, q, w, n_modes=2, n_azimuth=32)
+    assert sol.dropped_mode_norm < 1e-14
+    n = len(sol.nodes)
+    R0 = sol.R[0].real.reshape(n, 4, n, 4)[:, 0, :, 0]
+    T0 = sol.T[0].real.reshape(n, 4, n, 4)[:, 0, :, 0]
+    flux = 2 * (sol.nodes * sol.weights) @ (R0 + T0) + np.exp(-1.0 / sol.nodes)
+    assert np.max(np.abs(flux - 1.0)) < 1e-7
+
+    mie = O.MieScatterer(2.0 / (2 * math.pi), 1.5 + 0.01j, 1.0, 0.1, Ntheta=1801)
+    sol = D.solve(1.0, 0.9, D.TabulatedMatrix(mie.F11, mie.F12, mie.F33, mie.F34), q, w, n_modes=24,
+                  n_azimuth=128, n_doublings=24)
+    dphi = np.array([0.3, 1.1, 2.5])
+    Qm, Pm = np.diag([1.0, 1, 1, -1]), np.diag([1.0, 1, -1, -1])
+    for a, b in ((q[3], q[11]), (q[0], q[15]), (q[7], q[8])):
+        Rab = sol.reflection(a, b, dphi)
+        scale = np.abs(Rab).max()
+        assert np.abs(Rab - Qm @ np.swapaxes(sol.reflection(b, a, dphi), 1, 2) @ Qm).max() < 1e-12 * scale
+        assert np.abs(sol.reflection(a, b, -dphi) - Pm @ Rab @ Pm).max() < 1e-12 * scale
+        # and the polarisation is not trivial: the off-diagonal blocks carry weight
+        assert np.abs(Rab[:, 0, 1]).max() > 1e-2 * scale and np.abs(Rab[:, 2, 3]).max() > 1e-4 * scale
+
+
+@pytest.mark.parametrize("kind", ["rayleigh", "mie"])
+def test_oracle_first_order_equals_the_exact_single_scattering_matrix(O, kind):
+    """With one order and the first-collision depth on a midpoint grid the oracle's tally
+    is the single-scattering matrix to 1e-6 for all four incident states, which fixes
+    the frame relation D = diag(1, 1, -1, -1); the other sign of V fails for the Mie
+    matrix (its F34 couples U and V)."""
+    s = _case(O, kind)[0]
+    g = _geometry(O, s)
+    n = 1 << 14
+    cfg = O.Config(g, number_of_rays=n, compute_cb=False, maximum_scattering_times=1)
+    sol, mu0 = _solve(O, kind, cfg, n_doublings=0)  # no doubling: the layer's single scattering
+    got = np.array([O.simulate(cfg, g, I0, seed=3, rng_mode=1, threads=0)["Irt"] / n for I0 in STATES])
+    exp = _expected(sol, cfg, mu0)
+    scale = np.abs(exp).max()
+    err = np.abs(got - exp).max() / scale
+    print(f"{kind} first order: max |oracle - exact| / scale = {err:.2e}")
+    assert err < 1e-6
+    if kind == "mie":
+        # the same matrix with V of the other sign on both sides: the states' flipped
+        # vectors are combinations C of the states themselves, STATES Vflip = C STATES
+        Vflip = np.diag([1.0, 1, 1, -1])
+        C = STATES @ Vflip @ np.linalg.inv(STATES)
+        alt = np.einsum("ab,cs,sbjk->cajk", Vflip, C, exp)
+        assert np.abs(got - alt).max() / scale > 1e-2
+
+
+@pytest.fixture(scope="module", params=["rayleigh", "mie"])
+def all_orders(request, O):
+    """Slab tau = 1 at 30 degrees incidence with the reference's default 64 x 48 RT grid;
+    Rayleigh scatterers (omega 0.9) or Mie spheres x = 2, m = 1.5+0.01i (omega 0.951,
+    asymmetry 0.63). Per incident state 16 batches of 1 000 photons on disjoint Philox
+    ranges, with CB bins at theta_b = 0 and 0.001 rad (the incremental reciprocal-path
+    form, which equals the reference's walks to 1e-12); the RT tallies do not depend on
+    the CB settings."""
+    kind = request.param
+    s = _case(O, kind)[0]
+    g = _geometry(O, s)
+    nb, photons = 16, 1000
+    cfg = O.Config(g, number_of_rays=photons, compute_cb=True, thetab=np.array([0.0, 1e-3]), Nphib=2)
+    sol, mu0 = _solve(O, kind, cfg)
+    sol1 = _solve(O, kind, cfg, n_doublings=0)[0]  # the layer's single scattering, R1
+    runs = [[O.simulate(cfg, g, I0, seed=11 + i, threads=0, cb_form=1, photon_begin=b * photons,
+                        photon_count=photons) for i, I0 in enumerate(STATES)] for b in range(nb)]
+    return {"kind": kind, "cfg": cfg, "sol": sol, "sol1": sol1, "mu0": mu0, "nb": nb, "photons": photons,
+            "runs": runs}
+
+
+def test_oracle_rt_matches_the_exact_doubling_solution_at_all_orders(all_orders):
+    """Every bin, Stokes parameter and incident state (up to 49 152 comparisons) is scored
+    by z = (oracle - exact) / se: all |z| < 6 and mean z^2 < 1.6 (about 1.15 is expected
+    from 16 batch means); the reflected and transmitted fractions within 4 se; elements
+    that are exactly zero in the oracle (V from linear states in Rayleigh scattering) are
+    zero in the exact solution too."""
+    a = all_orders
+    kind, cfg, nb, photons = a["kind"], a["cfg"], a["nb"], a["photons"]
+    exp = _expected(a["sol"], cfg, a["mu0"])
+    bat = np.array([[r["Irt"] / photons for r in row] for row in a["runs"]])
+    mean = bat.mean(0)
+    se = bat.std(0, ddof=1) / math.sqrt(nb)
+    scale = np.abs(exp[:, 0]).max()
+    live = se > 0
+    z = (mean - exp)[live] / se[live]
+    print(f"{kind}: {live.sum()} comparisons, max |z| {np.abs(z).max():.2f}, mean z^2 {np.mean(z * z):.3f}, "
+          f"max |oracle - exact| / scale {np.abs(mean - exp).max() / scale:.2e}")
+    assert np.abs(z).max() < 6.0
+    assert np.mean(z * z) < 1.6
+    assert np.abs(exp[~live]).max(initial=0.0) < 1e-10 * scale
+    assert np.all(mean[~live] == 0.0)
+    h = cfg.Ntheta // 2
+    for name, sl in (("reflected", slice(h, None)), ("transmitted", slice(0, h))):
+        f = bat[:, 0, 0, sl].sum(axis=(1, 2))
+        zf = (f.mean() - exp[0, 0, sl].sum()) / (f.std(ddof=1) / math.sqrt(nb))
+        print(f"{kind} {name}: oracle {f.mean():.5f}, exact {exp[0, 0, sl].sum():.5f}, z {zf:.2f}")
+        assert abs(zf) < 4.0
+
+
+def test_oracle_cb_at_exact_backscatter_matches_reciprocity(all_orders):
+    """The CB tallies at theta_b = 0 against exact values. There the reciprocal paths'
+    phase difference vanishes, and the ensemble sum of their interference is fixed by
+    reciprocity: C = cyclical(L) with L = R - R1 at (mu0, mu0, pi) from the doubling
+    solution (tests/doubling.py). Per photon the ladder tally estimates
+    4 mu0 [R D I0]_1 and the CB intensity 4 mu0 [(R + C) D I0]_1 (the peel-off
+    normalisation of the RT bins without the quadrature weight). This checks the
+    reference's whole reciprocal-path machinery (src/cpu.jl:38-160: forward and backward
+    fields, the amplitude matrices, the scaling of the fields to the incoherent intensity
+    and the Ia / (Ia + Ib) share) at all orders, and the CB enhancement factor
+    Icb / ladder, for linearly and circularly polarised light and for unpolarised light
+    (which the reference carries as a circularly polarised field, src/utils.jl:122-134):
+    each within 4 se from the batch means."""
+    a = all_orders
+    kind, nb, photons, mu0 = a["kind"], a["nb"], a["photons"], a["mu0"]
+    sol = a["sol"]
+    R = sol.reflection(mu0, mu0, np.array([math.pi]))[0]
+    R1 = a["sol1"].reflection(mu0, mu0, np.array([math.pi]))[0]
+    C = D.cyclical(R - R1)
+    for i, I0 in enumerate(STATES):
+        lad = np.array([row[i]["ladder"][0, 0] / photons for row in a["runs"]])
+        icb = np.array([row[i]["Icb"][0, 0, 0] / photons for row in a["runs"]])
+        e_lad = 4 * mu0 * (R @ FRAME @ I0)[0]
+        e_icb = 4 * mu0 * ((R + C) @ FRAME @ I0)[0]
+        se = lambda v: v.std(ddof=1) / math.sqrt(nb)
+        zeta = icb / lad
+        z = [(lad.mean() - e_lad) / se(lad), (icb.mean() - e_icb) / se(icb),
+             (zeta.mean() - e_icb / e_lad) / se(zeta)]
+        print(f"{kind} I0 {I0}: ladder {lad.mean():.5f} (exact {e_lad:.5f}), CB {icb.mean():.5f} "
+              f"(exact {e_icb:.5f}), enhancement {zeta.mean():.4f} (exact {e_icb / e_lad:.4f}), "
+              f"z {np.round(z, 2)}")
+        assert np.all(np.abs(z) < 4.0)
+        assert 1.0 < e_icb / e_lad < 2.0
