@@ -40,8 +40,9 @@ TAU = 1.0
 
 
 def _case(O, kind):
-    if kind == "rayleigh":
-        s = O.RayleighScatterer(0.9, 1.0)
+    """(scatterer, F, azimuthal modes, azimuth samples) of a case."""
+    if kind.startswith("rayleigh"):
+        s = O.RayleighScatterer(0.8 if kind == "rayleigh_semi_infinite" else 0.9, 1.0)
         return s, D.rayleigh_matrix, 2, 16
     s = O.MieScatterer(2.0 / (2 * math.pi), 1.5 + 0.01j, 1.0, 0.1, Ntheta=1801)  # omega 0.951, g 0.63
     t = s.rounded_fp32()  # the oracle interpolates the FP32-rounded tables, as the device does
@@ -64,13 +65,18 @@ def _solve(O, kind, cfg, n_doublings=30):
     h = cfg.Ntheta // 2
     mu0 = abs(math.cos(THETA0))
     q, w = D.half_range_gauss(h)  # the bins' own half-range Gauss-Legendre nodes
-    sol = D.solve(TAU, s.omega, F, q, w, extra_mu=[mu0], n_modes=n_modes, n_azimuth=n_az,
+    tau = TAU
+    if kind == "rayleigh_semi_infinite":  # 60 optical depths: e^-46 of the light gets through
+        tau, n_doublings = 60.0, n_doublings + 6 if n_doublings else 0
+    sol = D.solve(tau, s.omega, F, q, w, extra_mu=[mu0], n_modes=n_modes, n_azimuth=n_az,
                   n_doublings=n_doublings)
     assert sol.dropped_mode_norm < 1e-6  # the azimuthal modes left out are negligible
     return sol, mu0
 
 
-def _geometry(O, s):
+def _geometry(O, kind, s):
+    if kind == "rayleigh_semi_infinite":
+        return O.PlaneGeometry(THETA0, 0.0, [O.Layer(d=-1.0, scatterer=s, tau=math.inf)])
     return O.PlaneGeometry(THETA0, 0.0, [O.Layer(d=TAU * s.kl, scatterer=s)])
 
 
@@ -112,7 +118,7 @@ def test_oracle_first_order_equals_the_exact_single_scattering_matrix(O, kind):
     the frame relation D = diag(1, 1, -1, -1); the other sign of V fails for the Mie
     matrix (its F34 couples U and V)."""
     s = _case(O, kind)[0]
-    g = _geometry(O, s)
+    g = _geometry(O, kind, s)
     n = 1 << 14
     cfg = O.Config(g, number_of_rays=n, compute_cb=False, maximum_scattering_times=1)
     sol, mu0 = _solve(O, kind, cfg, n_doublings=0)  # no doubling: the layer's single scattering
@@ -131,17 +137,19 @@ def test_oracle_first_order_equals_the_exact_single_scattering_matrix(O, kind):
         assert np.abs(got - alt).max() / scale > 1e-2
 
 
-@pytest.fixture(scope="module", params=["rayleigh", "mie"])
+@pytest.fixture(scope="module", params=["rayleigh", "mie", "rayleigh_semi_infinite"])
 def all_orders(request, O):
     """Slab tau = 1 at 30 degrees incidence with the reference's default 64 x 48 RT grid;
     Rayleigh scatterers (omega 0.9) or Mie spheres x = 2, m = 1.5+0.01i (omega 0.951,
-    asymmetry 0.63). Per incident state 16 batches of 1 000 photons on disjoint Philox
+    asymmetry 0.63); or a semi-infinite layer of Rayleigh scatterers (omega 0.8, the
+    reference's infinite Layer: unforced first flight, no lower boundary), whose exact
+    solution is the doubling carried to tau = 60. Per incident state 16 batches of 1 000 photons on disjoint Philox
     ranges, with CB bins at theta_b = 0 and 0.001 rad (the incremental reciprocal-path
     form, which equals the reference's walks to 1e-12); the RT tallies do not depend on
     the CB settings."""
     kind = request.param
     s = _case(O, kind)[0]
-    g = _geometry(O, s)
+    g = _geometry(O, kind, s)
     nb, photons = 16, 1000
     cfg = O.Config(g, number_of_rays=photons, compute_cb=True, thetab=np.array([0.0, 1e-3]), Nphib=2)
     sol, mu0 = _solve(O, kind, cfg)
@@ -154,9 +162,13 @@ def all_orders(request, O):
 
 def test_oracle_rt_matches_the_exact_doubling_solution_at_all_orders(all_orders):
     """Every bin, Stokes parameter and incident state (up to 49 152 comparisons) is scored
-    by z = (oracle - exact) / se: all |z| < 6 and mean z^2 < 1.6 (about 1.15 is expected
-    from 16 batch means); the reflected and transmitted fractions within 4 se; elements
-    that are exactly zero in the oracle (V from linear states in Rayleigh scattering) are
+    by z = (oracle - exact) / se: all |z| < 6, and mean z^2 < 2 as a loose gate against
+    a bias shared by many bins (about 1.15 is expected from 16 batch means, but all bins
+    see the same events, so the z are strongly correlated and their mean square
+    fluctuates far more than independent z's would: 1.36 is seen on the semi-infinite
+    layer at both 1.6e4 and 3.2e4 photons per state); the reflected and transmitted
+    fractions within 4 se; elements that are exactly zero in the oracle (V from linear
+    states in Rayleigh scattering, every transmission bin of the semi-infinite layer) are
     zero in the exact solution too."""
     a = all_orders
     kind, cfg, nb, photons = a["kind"], a["cfg"], a["nb"], a["photons"]
@@ -170,12 +182,15 @@ def test_oracle_rt_matches_the_exact_doubling_solution_at_all_orders(all_orders)
     print(f"{kind}: {live.sum()} comparisons, max |z| {np.abs(z).max():.2f}, mean z^2 {np.mean(z * z):.3f}, "
           f"max |oracle - exact| / scale {np.abs(mean - exp).max() / scale:.2e}")
     assert np.abs(z).max() < 6.0
-    assert np.mean(z * z) < 1.6
+    assert np.mean(z * z) < 2.0
     assert np.abs(exp[~live]).max(initial=0.0) < 1e-10 * scale
     assert np.all(mean[~live] == 0.0)
     h = cfg.Ntheta // 2
     for name, sl in (("reflected", slice(h, None)), ("transmitted", slice(0, h))):
         f = bat[:, 0, 0, sl].sum(axis=(1, 2))
+        if not np.any(f):  # the semi-infinite layer transmits nothing
+            assert abs(exp[0, 0, sl].sum()) < 1e-10
+            continue
         zf = (f.mean() - exp[0, 0, sl].sum()) / (f.std(ddof=1) / math.sqrt(nb))
         print(f"{kind} {name}: oracle {f.mean():.5f}, exact {exp[0, 0, sl].sum():.5f}, z {zf:.2f}")
         assert abs(zf) < 4.0
