@@ -18,7 +18,9 @@
 // slab of absorbing Mie spheres, and agreement at all orders with an exact vector
 // adding-doubling solution (tests/doubling.py): every RT bin's full Stokes vector for
 // four incident polarisation states, and the CB ladder, CB intensity and enhancement
-// factor at exact backscatter, where reciprocity fixes the interference term.
+// factor at exact backscatter, where reciprocity fixes the interference term; and for the
+// sphere, agreement at first order with an exact geometric integral (every RT bin, and
+// the CB bins near backscatter).
 //
 // Random numbers: the reference calls an unseeded rand(). Here every draw comes from
 // Philox4x32-10 keyed by (seed, instance) with counter (photon, event, attempt), and
