@@ -20,7 +20,8 @@
 // four incident polarisation states, and the CB ladder, CB intensity and enhancement
 // factor at exact backscatter, where reciprocity fixes the interference term; and for the
 // sphere, agreement at first order with an exact geometric integral (every RT bin, and
-// the CB bins near backscatter).
+// the CB bins near backscatter); and the CB cone at second order for Rayleigh scatterers,
+// exactly twice the ladder at exact backscatter and equal to an exact integral off it.
 //
 // Random numbers: the reference calls an unseeded rand(). Here every draw comes from
 // Philox4x32-10 keyed by (seed, instance) with counter (photon, event, attempt), and
