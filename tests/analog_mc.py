@@ -1,5 +1,5 @@
-"""An analog polarised Monte Carlo for a plane-parallel slab of Rayleigh scatterers or of
-spheres with a tabulated phase matrix, written for the tests independently of the oracle
+"""An analog polarised Monte Carlo for a plane-parallel slab, or a sphere, of Rayleigh
+scatterers or of particles with a tabulated phase matrix, written for the tests independently of the oracle
 and of the library.
 
 It follows photons the textbook way rather than the reference's way: no forced
@@ -48,6 +48,68 @@ class TabulatedPhase:
         return [np.interp(th, self.theta, f) for f in self.F]
 
 
+def _meridian_Q(S, k, e1):
+    """Q of Stokes vectors S (carried in the frame (e1, k x e1)) in the exit meridian
+    frame, whose first axis lies in the plane of z and k, normal to k."""
+    zhat = np.array([0.0, 0.0, 1.0])
+    ep = zhat[None, :] - k[:, 2:3] * k
+    ep /= np.linalg.norm(ep, axis=1)[:, None]
+    e2 = np.cross(k, e1)
+    chi = np.arctan2(np.einsum("ij,ij->i", ep, e2), np.einsum("ij,ij->i", ep, e1))
+    return _rot(S[:, 1], S[:, 2], chi)[0]
+
+
+def _scatter(S, k, e1, stay, rng, omega, phase):
+    """Scatters the photons `stay` in place: draws (Theta, phi) from the joint density of
+    the phase matrix for their Stokes vectors, turns the direction k and the frame vector
+    e1, applies the Mueller matrix and keeps the weight times omega."""
+    if phase is None:
+        # the scattering angle from P11 = 3/4 (1 + c^2), by rejection
+        c = np.empty(stay.size)
+        todo = np.arange(stay.size)
+        while todo.size:
+            cc = rng.uniform(-1.0, 1.0, todo.size)
+            ok = rng.uniform(0.0, 2.0, todo.size) < 1.0 + cc * cc
+            c[todo[ok]] = cc[ok]
+            todo = todo[~ok]
+        p11 = 0.75 * (1 + c * c)
+        p12 = -0.75 * (1 - c * c)
+        p33 = 1.5 * c
+        p34 = np.zeros_like(c)
+    else:
+        c = phase.sample_cos(rng.uniform(0.0, 1.0, stay.size))
+        p11, p12, p33, p34 = phase.elements(c)
+    I, Q, U, V = S[stay, 0], S[stay, 1], S[stay, 2], S[stay, 3]
+    # the azimuth of the scattering plane from the conditional density, by rejection
+    pol = np.sqrt(Q * Q + U * U) / I
+    bound = p11 + np.abs(p12) * pol
+    phi = np.empty(stay.size)
+    todo = np.arange(stay.size)
+    while todo.size:
+        ph = rng.uniform(0.0, 2 * math.pi, todo.size)
+        qr, _ = _rot(Q[todo], U[todo], ph)
+        dens = p11[todo] + p12[todo] * qr / I[todo]
+        ok = rng.uniform(0.0, 1.0, todo.size) * bound[todo] < dens
+        phi[todo[ok]] = ph[ok]
+        todo = todo[~ok]
+    Qr, Ur = _rot(Q, U, phi)
+    kk = k[stay]
+    e1o = e1[stay]
+    e2o = np.cross(kk, e1o)
+    e1p = np.cos(phi)[:, None] * e1o + np.sin(phi)[:, None] * e2o  # in the scattering plane
+    s = np.sqrt(np.maximum(1 - c * c, 0.0))
+    kn = c[:, None] * kk + s[:, None] * e1p
+    e1n = -s[:, None] * kk + c[:, None] * e1p
+    In = p11 * I + p12 * Qr
+    Qn = p12 * I + p11 * Qr
+    Un = p33 * Ur + p34 * V
+    Vn = -p34 * Ur + p33 * V
+    scale = omega * I / In
+    S[stay] = np.stack([In, Qn, Un, Vn], axis=1) * scale[:, None]
+    k[stay] = kn / np.linalg.norm(kn, axis=1)[:, None]
+    e1[stay] = e1n / np.linalg.norm(e1n, axis=1)[:, None]
+
+
 def run(tau, omega, n, rng, max_orders=200, batches=20, phase=None):
     """Normal incidence from above (k0 = -z), unpolarised light, slab z in [-tau, 0].
     `phase` is None for Rayleigh scatterers, else a TabulatedPhase.
@@ -88,13 +150,7 @@ def run(tau, omega, n, rng, max_orders=200, batches=20, phase=None):
                 out[key + "_mu"][b] += (w * mu).sum()
                 if key == "R":
                     out["R_mu2"][b] += (w * mu * mu).sum()
-                    # Q in the exit meridian frame: e_par in the plane of z and k, normal to k
-                    zhat = np.array([0.0, 0.0, 1.0])
-                    ep = zhat[None, :] - k[j, 2:3] * k[j]
-                    ep /= np.linalg.norm(ep, axis=1)[:, None]
-                    e2 = np.cross(k[j], e1[j])
-                    chi = np.arctan2(np.einsum("ij,ij->i", ep, e2), np.einsum("ij,ij->i", ep, e1[j]))
-                    Qm, _ = _rot(S[j, 1], S[j, 2], chi)
+                    Qm = _meridian_Q(S[j], k[j], e1[j])
                     out["R_Q"][b] += Qm.sum()
                     first = order[j] == 1
                     out["R1"][b] += w[first].sum()
@@ -104,51 +160,65 @@ def run(tau, omega, n, rng, max_orders=200, batches=20, phase=None):
             if stay.size == 0:
                 break
             z[stay] = zn[~(up | down)]
-            if phase is None:
-                # the scattering angle from P11 = 3/4 (1 + c^2), by rejection
-                c = np.empty(stay.size)
-                todo = np.arange(stay.size)
-                while todo.size:
-                    cc = rng.uniform(-1.0, 1.0, todo.size)
-                    ok = rng.uniform(0.0, 2.0, todo.size) < 1.0 + cc * cc
-                    c[todo[ok]] = cc[ok]
-                    todo = todo[~ok]
-                p11 = 0.75 * (1 + c * c)
-                p12 = -0.75 * (1 - c * c)
-                p33 = 1.5 * c
-                p34 = np.zeros_like(c)
-            else:
-                c = phase.sample_cos(rng.uniform(0.0, 1.0, stay.size))
-                p11, p12, p33, p34 = phase.elements(c)
-            I, Q, U, V = S[stay, 0], S[stay, 1], S[stay, 2], S[stay, 3]
-            # the azimuth of the scattering plane from the conditional density, by rejection
-            pol = np.sqrt(Q * Q + U * U) / I
-            bound = p11 + np.abs(p12) * pol
-            phi = np.empty(stay.size)
-            todo = np.arange(stay.size)
-            while todo.size:
-                ph = rng.uniform(0.0, 2 * math.pi, todo.size)
-                qr, _ = _rot(Q[todo], U[todo], ph)
-                dens = p11[todo] + p12[todo] * qr / I[todo]
-                ok = rng.uniform(0.0, 1.0, todo.size) * bound[todo] < dens
-                phi[todo[ok]] = ph[ok]
-                todo = todo[~ok]
-            Qr, Ur = _rot(Q, U, phi)
-            kk = k[stay]
-            e1o = e1[stay]
-            e2o = np.cross(kk, e1o)
-            e1p = np.cos(phi)[:, None] * e1o + np.sin(phi)[:, None] * e2o  # in the scattering plane
-            s = np.sqrt(np.maximum(1 - c * c, 0.0))
-            kn = c[:, None] * kk + s[:, None] * e1p
-            e1n = -s[:, None] * kk + c[:, None] * e1p
-            In = p11 * I + p12 * Qr
-            Qn = p12 * I + p11 * Qr
-            Un = p33 * Ur + p34 * V
-            Vn = -p34 * Ur + p33 * V
-            scale = omega * I / In
-            S[stay] = np.stack([In, Qn, Un, Vn], axis=1) * scale[:, None]
-            k[stay] = kn / np.linalg.norm(kn, axis=1)[:, None]
-            e1[stay] = e1n / np.linalg.norm(e1n, axis=1)[:, None]
+            _scatter(S, k, e1, stay, rng, omega, phase)
+            order[stay] += 1
+            alive[stay[order[stay] > max_orders]] = False
+        for key in out:
+            out[key][b] /= per
+    return out
+
+
+def run_sphere(tau, omega, n, rng, max_orders=2000, batches=20, phase=None):
+    """A sphere of optical radius tau lit along -z, unpolarised: photons enter at points
+    uniform over the projected disk, fly exponential free paths, and escape when a flight
+    is longer than the chord to the surface along their direction.
+
+    Returns per-batch estimates of, over the photons scattered at least once:
+      E, E_mu, E_mu2   the escaping fraction and its moments E[w mu], E[w mu^2] in the
+                       exit cosine mu (z component of the direction, in [-1, 1]),
+      E_Q              its Q in the exit meridian frame,
+      E1, E1_Q         the single-scattering parts of E and E_Q."""
+    out = {key: np.zeros(batches) for key in ("E", "E_mu", "E_mu2", "E_Q", "E1", "E1_Q")}
+    per = n // batches
+    for b in range(batches):
+        m = per
+        r = tau * np.sqrt(rng.uniform(0.0, 1.0, m))
+        psi = rng.uniform(0.0, 2 * math.pi, m)
+        x = np.stack([r * np.cos(psi), r * np.sin(psi), np.sqrt(tau * tau - r * r)], axis=1)
+        k = np.tile([0.0, 0.0, -1.0], (m, 1))
+        e1 = np.tile([1.0, 0.0, 0.0], (m, 1))
+        S = np.zeros((m, 4))
+        S[:, 0] = 1.0
+        order = np.zeros(m, dtype=int)
+        alive = np.ones(m, dtype=bool)
+        for _ in range(max_orders + 1):
+            idx = np.nonzero(alive)[0]
+            if idx.size == 0:
+                break
+            t = rng.exponential(1.0, idx.size)
+            kx = np.einsum("ij,ij->i", k[idx], x[idx])
+            xx = np.einsum("ij,ij->i", x[idx], x[idx])
+            d = -kx + np.sqrt(np.maximum(kx * kx + tau * tau - xx, 0.0))
+            out_ = t >= d
+            j = idx[out_]
+            j = j[order[j] > 0]  # unscattered photons are the direct beam
+            if j.size:
+                w = S[j, 0]
+                mu = k[j, 2]
+                Qm = _meridian_Q(S[j], k[j], e1[j])
+                first = order[j] == 1
+                out["E"][b] += w.sum()
+                out["E_mu"][b] += (w * mu).sum()
+                out["E_mu2"][b] += (w * mu * mu).sum()
+                out["E_Q"][b] += Qm.sum()
+                out["E1"][b] += w[first].sum()
+                out["E1_Q"][b] += Qm[first].sum()
+            alive[idx[out_]] = False
+            stay = idx[~out_]
+            if stay.size == 0:
+                break
+            x[stay] += t[~out_, None] * k[stay]
+            _scatter(S, k, e1, stay, rng, omega, phase)
             order[stay] += 1
             alive[stay[order[stay] > max_orders]] = False
         for key in out:
