@@ -1,6 +1,6 @@
 """An analog polarised Monte Carlo for a plane-parallel slab, or a sphere, of Rayleigh
-scatterers or of particles with a tabulated phase matrix, written for the tests independently of the oracle
-and of the library.
+scatterers or of particles with a tabulated phase matrix, written for the tests
+independently of the oracle and of the library.
 
 It follows photons the textbook way rather than the reference's way: no forced
 collisions, no peel-off and no weight renormalisation. A photon flies an exponential
