@@ -160,3 +160,28 @@ def test_julia_ccalls_are_declared_in_the_header():
     declared = set(re.findall(r"\b(mcrt_\w+)\s*\(", _strip_comments(open(HEADER, encoding="utf-8").read())))
     called = set(re.findall(r"ccall\(\(:(\w+),\s*libmcrt\)", open(JULIA, encoding="utf-8").read()))
     assert called and called <= declared, called - declared
+
+
+def test_julia_binding_reads_only_fields_the_reference_defines():
+    """Every field the binding reads from the reference's objects (cfg::Config, g a
+    geometry, l a Layer, s a scatterer) is a field of the reference's type, by the names
+    in tests/golden/reference_fields.json (extracted from the reference's sources by
+    make_reference_fields.py beside it): a misspelt or missing field would only fail
+    when Julia runs the binding."""
+    import json
+
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_fields.json"), encoding="utf-8"))["fields"]
+    allowed = {
+        "cfg": set(ref["Config"]),
+        "g": set(ref["PlaneGeometry"]) | set(ref["SphereGeometry"]),
+        "l": set(ref["Layer"]),
+        "s": set(ref["RayleighScatterer"]) | set(ref["MieScatterer"]),
+    }
+    src = open(JULIA, encoding="utf-8").read()
+    seen = {}
+    for obj, field in re.findall(r"(?<![\w.])(cfg|g|l|s)\.([^\W\d]\w*)", src):
+        seen.setdefault(obj, set()).add(field)
+    assert {"cfg", "g", "l", "s"} <= set(seen)
+    for obj, names in seen.items():
+        assert names <= allowed[obj], (obj, sorted(names - allowed[obj]))
+    assert len(seen["cfg"]) >= 15  # the binding marshals the whole Config
