@@ -261,3 +261,45 @@ def test_arrow_writer_uses_the_reference_columns(M, tmp_path):
     assert t.column_names == ["θ"] + [f"s{a}{b}" for a in range(1, 5) for b in range(1, 5)]
     assert all(f.type == pa.float64() for f in t.schema)
     assert t.column("θ").to_pylist() == [10.0, 20.0] and t.column("s44").to_pylist() == [4.4, -4.4]
+
+
+def test_host_mirrors_match_the_reference_source(M, O):
+    """The Python mirrors of the reference's types (the library's host package and the
+    oracle's own) against the reference's text, as extracted into
+    tests/golden/reference_fields.json by make_reference_fields.py: Config's literal
+    defaults, the default CB angles (DEFAULT_THEB, src/config.jl:3-53) and the exact
+    ArgumentError messages of validate (src/geometries/plane.jl:52-62, sphere.jl:35-37)."""
+    import mcrt_gb300.model as model
+
+    ref = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                      "reference_fields.json"), encoding="utf-8"))
+    d = ref["config_defaults"]
+    names = {"number_of_rays": "number_of_rays", "minimum_intensity": "minimum_intensity",
+             "maximum_scattering_times": "maximum_scattering_times", "compute_cb": "compute_cb",
+             "τ₀": "tau0", "Nϕ": "Nphi", "Nθ": "Ntheta", "Nϕb": "Nphib"}
+    deg = np.array(ref["default_theb_degrees"])
+    for Mod in (M, O):
+        ray = Mod.RayleighScatterer(0.99, 1.0)
+        cfg = Mod.Config(Mod.PlaneGeometry(math.pi, 0.0, [Mod.Layer(d=1.0, scatterer=ray)]))
+        for jl, py in names.items():
+            assert getattr(cfg, py) == d[jl], (Mod.__name__, jl)
+        assert cfg.Nthetab == len(deg)
+        assert np.allclose(np.arccos(np.clip(cfg.costhetab, -1, 1)), np.pi / 180.0 * deg, rtol=0, atol=2e-8)
+    assert M.Config(M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=1.0, scatterer=M.RayleighScatterer(0.99, 1.0))])
+                    ).maximum_threads == d["maximum_threads"]
+    assert list(model.DEFAULT_THEB_DEG) == list(deg) and list(O.DEFAULT_THEB_DEG) == list(deg)
+
+    ray = M.RayleighScatterer(0.99, 1.0)
+    bad = [M.PlaneGeometry(1.0, 0.0, [M.Layer(d=1.0, scatterer=ray)]),
+           M.PlaneGeometry(math.pi, 7.0, [M.Layer(d=1.0, scatterer=ray)]),
+           M.PlaneGeometry(math.pi, 0.0, []),
+           M.PlaneGeometry(math.pi, 0.0, [M.Layer(d=-1, scatterer=ray, tau=math.inf), M.Layer(d=1, scatterer=ray)])]
+    got = []
+    for g in bad:
+        with pytest.raises(ValueError) as e:
+            g.validate()
+        got.append(str(e.value))
+    assert got == ref["validate_messages"]["PlaneGeometry"]
+    with pytest.raises(ValueError) as e:
+        M.SphereGeometry(R=0.0, scatterer=ray).validate()
+    assert [str(e.value)] == ref["validate_messages"]["SphereGeometry"]
