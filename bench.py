@@ -59,7 +59,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=1 << 22, help="photons per step per GPU")
     ap.add_argument("--fp64-sample", type=int, default=1 << 16)
-    ap.add_argument("--cpu-sample", type=int, default=2000)
+    ap.add_argument("--cpu-sample", type=int, default=2000,
+                    help="photons per step of the reference arm (and its warm-up, a quarter)")
+    ap.add_argument("--cpu-baseline-sample", type=int, default=20000,
+                    help="photons of the GPU arm's cpu_baseline leg: about 15 s on 16 host cores")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64, CPU and serving legs")
     ap.add_argument("--case", type=int, default=0,
                     help="run one FP32 launch of the workload with this many photons and exit "
@@ -503,7 +506,7 @@ def main():
         ref_threads, ref_ppt = 8192, 2
         vplain_ref, ref_blocks = plain_rate(ref_threads, ref_threads * ref_ppt)
         v64 = np64 / (r64["stats"]["kernel_ms"] / 1e3)
-        cpu_v, cores, cpu_dt = cpu_oracle_rate(args.cpu_sample)
+        cpu_v, cores, cpu_dt = cpu_oracle_rate(args.cpu_baseline_sample)
         serve = serve_leg(M, ctx, args.serve_requests, args.serve_scale) if args.serve_requests > 0 else None
         batch = batch_leg(M, ctx)
         others = other_workloads_leg(M, ctx)
@@ -530,7 +533,7 @@ def main():
             "fp32_over_fp64_plain_reference_launch": value / world / vplain_ref,
             "fp32_over_fp64_persistent": value / world / v64,
             "cpu_baseline": {"value": cpu_v, "unit": "paths/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.cpu_sample} photons of the same workload, FP64, "
+                             "sample": f"{args.cpu_baseline_sample} photons of the same workload, FP64, "
                                        f"{cpu_dt:.1f} s"},
         }
 
