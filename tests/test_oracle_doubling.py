@@ -282,3 +282,37 @@ def test_oracle_cb_enhancement_on_the_headline_mie_slab_is_exact(O):
         assert abs(zeta / (e_icb / e_lad) - 1) < 0.01
         assert abs(lad.mean() / e_lad - 1) < 0.08 and abs(icb.mean() / e_icb - 1) < 0.08
         assert 1.0 < e_icb / e_lad < 2.0
+
+
+def test_run_rt_assembly_of_the_exact_tallies_is_the_exact_matrix(M, O):
+    """run_rt's Mueller assembly for a plane (src/MonteCarloRadiativeTransfer.jl:186-291:
+    half differences of the six polarised states' tallies, scaled by
+    1 / |4 cos(theta) inorm|), restated in tests/helpers.py and matched by the device
+    epilogue at 1e-9 in the GPU tests, applied to the exact expected tallies
+    4 |mu| inorm D R D I0 (the doubling solution, all orders), returns exactly
+    s_ab = (D R D)_ab, the reflection and transmission matrices in the doubling papers'
+    normalisation, in the reference's frame. Deterministic: 1e-12. With the oracle's
+    tallies matching the exact ones (the tests above), this fixes what run_rt's
+    s11 ... s44 columns are."""
+    from helpers import assemble_run_rt
+
+    for kind in ("rayleigh", "mie"):
+        s = _case(O, kind)[0]
+        g = _geometry(O, kind, s)
+        cfg = O.Config(g, number_of_rays=1, compute_cb=False)
+        sol, mu0 = _solve(O, kind, cfg)
+        phi = np.arctan2(cfg.sinphi, cfg.cosphi)
+        exact = np.zeros((4, 4, cfg.Ntheta, cfg.Nphi))
+        for j, mu in enumerate(cfg.costheta):
+            Rj = sol.reflection(mu, mu0, phi) if mu > 0 else sol.transmission(-mu, mu0, phi)
+            exact[:, :, j, :] = np.moveaxis(FRAME @ Rj @ FRAME, 0, -1)
+        tally = exact * (4 * np.abs(cfg.costheta) * cfg.inorm)[None, None, :, None]
+
+        def sim(I, _):
+            Irt = np.einsum("abjk,b->ajk", tally, np.asarray(I, float))
+            return (0.0, 0.0, Irt[0, cfg.Ntheta // 2:].sum(), Irt[0, :cfg.Ntheta // 2].sum(), 0.0, Irt,
+                    np.zeros((4, cfg.Nthetab, cfg.Nphib)))
+
+        shape_g = M.PlaneGeometry(THETA0, 0.0, [M.Layer(d=1.0, scatterer=M.RayleighScatterer(0.9, 1.0))])
+        MRT = assemble_run_rt(cfg, shape_g, sim)[0]
+        assert np.abs(MRT - exact).max() < 1e-12 * np.abs(exact).max(), kind

@@ -114,3 +114,41 @@ def test_oracle_sphere_first_order_matches_the_exact_integral(O, kind):
     print(f"{kind} sphere CB: max |z| {np.abs(zc).max():.2f}, at exact backscatter oracle "
           f"{cb.mean(0)[0, 0]:.5f}, exact {exp_cb[0]:.5f}")
     assert np.abs(zc).max() < 5.0
+
+
+@pytest.mark.parametrize("kind", ["rayleigh", "mie"])
+def test_run_rt_sphere_assembly_of_the_exact_first_order(M, O, kind):
+    """run_rt's assembly for a sphere (src/MonteCarloRadiativeTransfer.jl:87-184: the two
+    states [1,-1,0,0] and [1,0,0,-1], the azimuths 0, 45, ..., 315 degrees combined into
+    the columns, renormalised by the scattered fraction Gdt + Gref and the quadrature
+    weight), restated in tests/helpers.py and matched by the device epilogue at 1e-9 in
+    the GPU tests, applied to the exact first-order tallies above, returns exactly
+    omega G(mu) / (Gdt + Gref) F(Theta): the scattering matrix [[F11, F12, 0, 0],
+    [F12, F11, 0, 0], [0, 0, F33, F34], [0, 0, -F34, F33]] in the scattering plane,
+    which the reference's frame leaves as it is (D F D = F). Deterministic: 1e-12."""
+    from helpers import assemble_run_rt
+
+    s, F, tau = _case(O, kind)
+    g = O.SphereGeometry(R=tau * s.kl, scatterer=s)
+    cfg = O.Config(g, number_of_rays=1, compute_cb=False, Ntheta=16, Nphi=8)
+    Gv = geometric_factor(tau, cfg.costheta)
+    phi = np.arctan2(cfg.sinphi, cfg.cosphi)
+    Z = np.array([[D.phase_matrix(mu, p, -1.0, 0.0, F) for p in phi] for mu in cfg.costheta])
+    tally = np.einsum("ab,jkbc,cd->adjk", FRAME, Z, FRAME) * (s.omega * cfg.inorm * Gv)[None, None, :, None]
+    direct = (1 - (1 + 2 * tau) * math.exp(-2 * tau)) / (2 * tau * tau)  # mean e^{-chord} over the disk
+
+    def sim(I, _):
+        Irt = np.einsum("abjk,b->ajk", tally, np.asarray(I, float))
+        return (direct, 0.0, Irt[0].sum(), 0.0, 0.0, Irt, np.zeros((4, cfg.Nthetab, cfg.Nphib)))
+
+    shape_g = M.SphereGeometry(R=2.0, scatterer=M.RayleighScatterer(0.9, 1.0))
+    MRT, _, G = assemble_run_rt(cfg, shape_g, sim)
+    c = -cfg.costheta  # cos(Theta) for the exit cosine mu, light incident along -z
+    F11, F12, F33, F34 = F(c)
+    Fm = np.zeros((4, 4, cfg.Ntheta))
+    Fm[0, 0] = Fm[1, 1] = F11
+    Fm[0, 1] = Fm[1, 0] = F12
+    Fm[2, 2] = Fm[3, 3] = F33
+    Fm[2, 3], Fm[3, 2] = F34, -F34
+    expect = Fm * (s.omega * Gv / (G[0] + G[2]))[None, None, :]
+    assert np.abs(MRT - expect).max() < 1e-12 * np.abs(expect).max()
