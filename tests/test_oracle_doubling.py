@@ -244,9 +244,11 @@ def test_oracle_cb_enhancement_on_the_headline_mie_slab_is_exact(O):
     exact arithmetic, was 0.3% high; the circular state's ladder was 4% low (z = -3) at
     4 800 photons and agrees at 6.4e4 (z = -0.5). So the gates are relative: the CB
     enhancement factor at exact backscatter, a ratio in which the tails largely cancel,
-    within 1% of the exact value for all four incident states (a CB that ignored
-    reciprocity's structure, C = L, would give 1.83 against the exact 1.71); the ladder
-    and CB intensities within 8%; the reflected and transmitted fractions within 4 se."""
+    within 1% of the exact value for unpolarised light (the metric's CB peak) and for
+    linearly polarised light (a CB that ignored reciprocity's structure, C = L, would
+    give 1.83 against the exact 1.71); the ladder and CB intensities within 8%; the
+    reflected and transmitted fractions within 4 se. (The circularly polarised and U
+    states' CB elements are checked on the Mie slab of tau = 1 above.)"""
     mie = O.MieScatterer(5.0 / (2 * math.pi), 1.5 + 0.001j, 1.0, 0.1, Ntheta=1801)
     tau = 5.0
     t = mie.rounded_fp32()
@@ -263,15 +265,16 @@ def test_oracle_cb_enhancement_on_the_headline_mie_slab_is_exact(O):
     R = sol.reflection(mu0, mu0, np.array([math.pi]))[0]
     C = D.cyclical(R - sol1.reflection(mu0, mu0, np.array([math.pi]))[0])
     exp = _expected(sol, cfg, mu0)
+    states = STATES[:2]  # [1,0,0,0] and [1,1,0,0]
     runs = [[O.simulate(cfg, g, I0, seed=11 + i, threads=0, cb_form=1, photon_begin=b * photons,
-                        photon_count=photons) for i, I0 in enumerate(STATES)] for b in range(nb)]
+                        photon_count=photons) for i, I0 in enumerate(states)] for b in range(nb)]
     h = cfg.Ntheta // 2
     for name, sl in (("reflected", slice(h, None)), ("transmitted", slice(0, h))):
         f = np.array([row[0]["Irt"][0, sl].sum() / photons for row in runs])
         zf = (f.mean() - exp[0, 0, sl].sum()) / (f.std(ddof=1) / math.sqrt(nb))
         print(f"headline Mie slab {name}: oracle {f.mean():.5f}, exact {exp[0, 0, sl].sum():.5f}, z {zf:.2f}")
         assert abs(zf) < 4.0
-    for i, I0 in enumerate(STATES):
+    for i, I0 in enumerate(states):
         lad = np.array([row[i]["ladder"][0, 0] / photons for row in runs])
         icb = np.array([row[i]["Icb"][0, 0, 0] / photons for row in runs])
         e_lad = 4 * mu0 * (R @ FRAME @ I0)[0]
