@@ -3,12 +3,13 @@ written for the tests independently of the oracle and of the library.
 
 It gives the exact (to quadrature accuracy) reflection and diffuse transmission matrices
 R(mu, mu0, phi - phi0) and T(mu, mu0, phi - phi0) of polarised light at all scattering
-orders, by the published doubling method: Hansen & Travis, Space Sci. Rev. 16 (1974)
-527, sec. 3 (the adding equations in kernel form) and de Haan, Bosma & Hovenier,
-Astron. Astrophys. 183 (1987) 371 (the same for the full Stokes vector, mode by mode in
-azimuth). The normalisation is theirs: for a parallel beam of net flux pi F per unit
-area normal to the beam, incident at cosine mu0, the reflected radiance is
-I(mu, phi) = mu0 R(mu, mu0, phi - phi0) F.
+orders, by the published adding-doubling method: Hansen & Travis, "Light scattering in
+planetary atmospheres", Space Sci. Rev. (1974) (the adding equations in kernel form),
+and de Haan, Bosma & Hovenier, "The adding method for multiple scattering calculations
+of polarized light", Astron. Astrophys. (1987) (the same for the full Stokes vector,
+mode by mode in azimuth). The normalisation is theirs: for a parallel beam of net flux
+pi F per unit area normal to the beam, incident at cosine mu0, the reflected radiance
+is I(mu, phi) = mu0 R(mu, mu0, phi - phi0) F.
 
 How it is built:
 - Directions are (mu, phi), k = (sqrt(1 - mu^2) cos phi, sqrt(1 - mu^2) sin phi, mu),
@@ -135,14 +136,17 @@ def fourier_modes(mu_out, mu_in, F, n_modes, n_azimuth):
 
 
 class DoublingSolution:
-    """R and T (with R* and T* from below) per azimuthal mode at the node cosines."""
+    """R and T (with R* and T* from below) per azimuthal mode at the node cosines
+    `nodes` (quadrature `weights`, zero for the added cosines); `dropped_mode_norm` is the
+    largest azimuthal mode of the phase matrix left out."""
 
-    def __init__(self, mu, modes_R, modes_T, modes_Rs, modes_Ts, tau):
-        self.mu, self.tau = mu, tau
+    def __init__(self, nodes, weights, modes_R, modes_T, modes_Rs, modes_Ts, tau, dropped_mode_norm):
+        self.nodes, self.weights, self.tau = nodes, weights, tau
         self.R, self.T, self.Rs, self.Ts = modes_R, modes_T, modes_Rs, modes_Ts
+        self.dropped_mode_norm = dropped_mode_norm
 
     def _index(self, m):
-        i = np.flatnonzero(np.isclose(self.mu, m, rtol=0, atol=1e-14))
+        i = np.flatnonzero(np.isclose(self.nodes, m, rtol=0, atol=1e-14))
         if len(i) == 0:
             raise KeyError(f"cosine {m} is not a node of this solution")
         return int(i[0])
@@ -203,15 +207,13 @@ def solve(tau, omega, F, quad_mu, quad_w, extra_mu=(), n_modes=2, n_azimuth=16, 
         R, T, Rs, Ts = [np.stack(v) for v in zip(*[_double(R[m], T[m], Rs[m], Ts[m], e, Mw, I)
                                                    for m in range(R.shape[0])])]
         d *= 2.0
-    sol = DoublingSolution(u, R, T, Rs, Ts, tau)
-    sol.dropped_mode_norm = dropped
-    sol.nodes, sol.weights = u, W
-    return sol
+    return DoublingSolution(u, W, R, T, Rs, Ts, tau, dropped)
 
 
 def _double(R, T, Rs, Ts, e, Mw, I):
-    """One doubling step in kernel form (Hansen & Travis 1974, eqs. 87-89, extended to
-    incidence from below): layers a and b are the same layer."""
+    """One doubling step with the adding equations in kernel form (Hansen & Travis
+    1974), for incidence from above and, with the roles of the two sides exchanged, from
+    below: layers a and b are the same layer."""
     def add(Ra, Ta, Rsa, Tsa):
         # light from above on a, then b = the same layer
         Q = (Rsa * Mw) @ Ra
@@ -251,7 +253,8 @@ def cyclical_map():
     vector; C is the ensemble sum of those cross terms as L is the sum of the paths'
     Mueller matrices. Both are linear in the paths' coherency S (x) S*, so C is a linear
     function of L, found here by least squares over random Jones matrices. Its (1, 1)
-    element is (L11 + L22 - L33 + L44) / 2 (Mishchenko, J. Opt. Soc. Am. A 9 (1992) 978)."""
+    element is (L11 + L22 - L33 + L44) / 2, the relation Mishchenko derived for exact
+    backscattering (J. Opt. Soc. Am. A, 1992)."""
     E = [np.array([1, 0], complex), np.array([0, 1], complex), np.array([1, 1], complex) / math.sqrt(2),
          np.array([1, 1j], complex) / math.sqrt(2)]
     Sv_inv = np.linalg.inv(np.array([_cross_stokes(e, e) for e in E]).T)

@@ -86,7 +86,8 @@ def test_doubling_solver_conserves_energy_and_obeys_reciprocity(O):
     beyond 2; and for a Mie phase matrix, at all orders, the reciprocity relation
     R(mu_a, mu_b, dphi) = Q R(mu_b, mu_a, dphi)^T Q with Q = diag(1, 1, 1, -1) and the
     mirror relation R(mu, mu0, -dphi) = P R(mu, mu0, dphi) P with P = diag(1, 1, -1, -1)
-    (Hovenier, van der Mee & Domke, Transfer of Polarized Light, 2004, sec. 5.3; the
+    (the reciprocity and mirror-symmetry relations of polarised reflection, e.g. Hovenier,
+    van der Mee & Domke, Transfer of Polarized Light in Planetary Atmospheres, 2004; the
     signs are those of a right-handed meridian frame)."""
     q, w = D.half_range_gauss(16)
     sol = D.solve(1.0, 1.0, D.rayleigh_matrix, q, w, n_modes=2, n_azimuth=32)
