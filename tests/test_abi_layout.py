@@ -185,3 +185,25 @@ def test_julia_binding_reads_only_fields_the_reference_defines():
     for obj, names in seen.items():
         assert names <= allowed[obj], (obj, sorted(names - allowed[obj]))
     assert len(seen["cfg"]) >= 15  # the binding marshals the whole Config
+
+
+def test_julia_parity_script_uses_the_reference_constructors():
+    """julia/test_binding.jl builds the reference's types with keyword constructors
+    (the types are Base.@kwdef structs): every keyword is a field of that type (for
+    MieScatterer, the keywords of its outer constructor, Nθ and random_points, are fields
+    too), and every field it reads from them exists (names from
+    tests/golden/reference_fields.json)."""
+    import json
+
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_fields.json"), encoding="utf-8"))["fields"]
+    src = open(os.path.join(os.path.dirname(JULIA), "test_binding.jl"), encoding="utf-8").read()
+    checked = 0
+    # innermost calls only, so that a nested constructor's keywords stay its own
+    for name, args in re.findall(r"MCRT\.(\w+)\(([^()]*)\)", src):
+        if name not in ref:  # a function (simulate), not one of the types
+            continue
+        for kw in re.findall(r"(?:^|[,;]\s*)([^\W\d]\w*)\s*=(?!=)", args):
+            assert kw in ref[name], (name, kw)
+            checked += 1
+    assert checked >= 8
+    assert "kl" in ref["MieScatterer"] and "layers" in ref["PlaneGeometry"]  # mie.kl, plane.layers
