@@ -19,7 +19,9 @@ oracle on identical streams).
   * the reflected fraction is 0.17% below the exact one (and the transmitted 0.14%
     above): Theta is drawn from csrn, a 1000-point inverse CDF (src/utils.jl:263-287),
     whose distribution is slightly more forward-peaked than the tabulated F11 the peel-off
-    and the exact solution use (its mean cosine is higher by 7e-4).
+    and the exact solution use (its mean cosine is higher by 7e-4); an analog Monte Carlo
+    drawing Theta both ways (analog_mc.CsrnPhase against TabulatedPhase) shows the same
+    shift.
 """
 import math
 
