@@ -89,7 +89,8 @@ def test_fp32_arccos_meets_its_published_error_bound():
     for c in a[1:]:
         p = (p * ax + c).astype(np.float32)
     y = np.maximum(f(1) - ax, f(0))
-    r = np.where(y > 0, (y * (f(1) / np.sqrt(y)) * p).astype(np.float32), f(0))
+    with np.errstate(divide="ignore", invalid="ignore"):  # y = 0 takes the other branch
+        r = np.where(y > 0, (y * (f(1) / np.sqrt(y)) * p).astype(np.float32), f(0))
     th = np.where(x < 0, f(3.14159265358979) - r, r).astype(np.float32)
     err = np.abs(th.astype(np.float64) - np.arccos(x.astype(np.float64)))
     assert err.max() < 5e-7, err.max()
