@@ -266,8 +266,9 @@ def cyclical_map():
         Sr = J @ S.T @ J
         A.append((np.array([_cross_stokes(S @ e, S @ e) for e in E]).T @ Sv_inv).ravel())
         B.append((np.array([_cross_stokes(S @ e, Sr @ e) for e in E]).T @ Sv_inv).ravel())
-    Phi, _, rank, _ = np.linalg.lstsq(np.array(A), np.array(B), rcond=None)
-    assert rank == 16
+    A, B = np.array(A), np.array(B)
+    Phi, _, rank, _ = np.linalg.lstsq(A, B, rcond=None)
+    assert rank == 16 and np.abs(A @ Phi - B).max() < 1e-10  # exactly linear in the coherency
     return Phi
 
 

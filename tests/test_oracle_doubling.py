@@ -111,6 +111,11 @@ def test_doubling_solver_conserves_energy_and_obeys_reciprocity(O):
         # and the polarisation is not trivial: the off-diagonal blocks carry weight
         assert np.abs(Rab[:, 0, 1]).max() > 1e-2 * scale and np.abs(Rab[:, 2, 3]).max() > 1e-4 * scale
 
+    # the interference map of exact backscatter: its (1, 1) element is Mishchenko's
+    # (L11 + L22 - L33 + L44) / 2 for any ladder matrix L
+    L = np.random.default_rng(1).normal(size=(4, 4))
+    assert abs(D.cyclical(L)[0, 0] - (L[0, 0] + L[1, 1] - L[2, 2] + L[3, 3]) / 2) < 1e-12
+
 
 @pytest.mark.parametrize("kind", ["rayleigh", "mie"])
 def test_oracle_first_order_equals_the_exact_single_scattering_matrix(O, kind):
